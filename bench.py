@@ -1,0 +1,329 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 tetra-mesh step: prints ONE JSON line.
+
+Workload (default): the large plain cell — Kuhn sphere of radius 64 (6,594,816 tetra,
+1,138,197 nodes), Mooney-Rivlin C10 = 5e-4, C01 = 1e-4, K = 1e-2 with the finite-strain
+viscoplastic law (yield 2e-4, viscosity 5e-2), rigid substrate, spherical indenter of radius 16
+descending 1e-4 per step, damping 1e-2, FP32 kernels. A "step" is one time step of the cell.
+
+  value      tetra-steps/s over --steps steps with the state resident in HBM, timed by CUDA
+             events on the library's stream (nfx_time_steps); whole job over all ranks.
+  e2e        the same metric through the C ABI with host buffers: per output interval of 100
+             steps the indenter positions are uploaded from pinned host memory (the reference's
+             per-step beforeTimeStep callable) and node positions plus the force row are read
+             back into pinned host memory (the reference's writeVTK readback).
+  roofline   the element pass (dominant kernel): algorithmic bytes per launch / its average
+             CUDA-event duration (nfx_profile_steps), against MEASURED_PEAKS.json hbm_gbs.
+  cpu_baseline  the oracle port of the reference kernels (FP64, OpenMP, all host cores) on a
+             bounded sample of the same workload.
+
+--impl reference times the CPU implementation of the path (the oracle port of the reference's
+kernels; the reference itself needs an OpenCL runtime that is not installed) on the same
+workload and metric. Multi-GPU (torchrun): the single-cell path does not shard, so every rank
+runs an independent replica ("replicas only"); value sums the ranks' work over the slowest rank.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from nofluidx3d_gb300 import workloads  # noqa: E402
+
+# Algorithmic bytes per tetra-step of the element pass, counted as the unique state a fused
+# schedule must stream from HBM per step: connectivity 16 + Dm^-1 36 + V0 4 = 56 B; the
+# viscoplastic state adds Fp 36 read + 36 written and the plastic strain 4 + 4 = 80 B.
+ELEM_BYTES = {"nh": 56.0, "mr": 56.0, "mr_vp": 136.0}
+# Per node and step: position, velocity and previous force, each 12 B read + 12 B written.
+NODE_BYTES = 72.0
+
+
+def load_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def load_traffic(workload_key: str) -> float | None:
+    """DRAM bytes per tetra of the element pass from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", f"tet_pass_{workload_key}.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_tetra:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict | None:
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = max(smax, float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        return world, rank, local, dist
+    return 1, 0, 0, None
+
+
+def reduce_max(dist, x: float, local: int) -> float:
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{local}")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist, local: int):
+    if dist is not None:
+        import torch
+
+        dist.barrier(device_ids=[local])
+        torch.cuda.synchronize(local)
+
+
+def cpu_baseline(w, sample_seconds: float, threads: int = 0) -> dict:
+    """The oracle port (FP64, OpenMP over work-items) on a bounded number of whole time steps."""
+    import oracle as O
+    from tests.helpers import oracle_problem
+
+    mesh = w.mesh()
+    st = O.State(oracle_problem(w, mesh), "f64")
+    th = threads or O.max_threads()
+    t0 = time.perf_counter()
+    st.run(1, parallel=True, threads=th)  # warm-up (page-in, thread pool)
+    one = time.perf_counter() - t0
+    n = max(1, int(sample_seconds / max(one, 1e-6)))
+    t0 = time.perf_counter()
+    st.run(n, parallel=True, threads=th)
+    dt = time.perf_counter() - t0
+    return {"value": mesh.num_tetra * n / dt, "unit": "tetra-steps/s", "cores": th, "kind": "port",
+            "sample": f"{n} whole time steps of the {w.name} cell ({mesh.num_tetra} tetra), FP64, "
+                      f"{th} OpenMP threads, after 1 warm-up step"}
+
+
+def run_reference(args):
+    world, rank, local, dist = dist_setup()
+    if rank != 0:
+        return
+    w = workloads.WORKLOADS[args.workload]()
+    import oracle as O
+    from tests.helpers import oracle_problem
+
+    mesh = w.mesh()
+    st = O.State(oracle_problem(w, mesh), "f64")
+    th = O.max_threads()
+    for _ in range(min(args.warmup, 1)):
+        st.run(1, parallel=True, threads=th)
+    budget = args.reference_seconds
+    done, t0 = 0, time.perf_counter()
+    while done < args.steps and (time.perf_counter() - t0) < budget:
+        st.run(1, parallel=True, threads=th)
+        done += 1
+    dt = time.perf_counter() - t0
+    val = mesh.num_tetra * done / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "tetra-steps/s", "n_gpus": world,
+        "steps": done, "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * dt / max(done, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": w.name, "tets": mesh.num_tetra, "nodes": mesh.num_points,
+                   "implementation": "oracle port of the reference's OpenCL kernels, OpenMP"},
+        "cpu_baseline": {"value": val, "unit": "tetra-steps/s", "cores": th, "kind": "port",
+                         "sample": f"{done} whole time steps (of {args.steps} requested, capped at {budget:.0f} s)"},
+        "e2e": {"value": val, "unit": "tetra-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+METRIC = "tetra-steps/s + % HBM peak, 1 GB300"
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--warmup", type=int, default=200)
+    ap.add_argument("--impl", default="nfx", choices=["nfx", "reference"])
+    ap.add_argument("--workload", default="plain-large", choices=sorted(workloads.WORKLOADS))
+    ap.add_argument("--profile-steps", type=int, default=20)
+    ap.add_argument("--e2e-steps", type=int, default=1000)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--reference-seconds", type=float, default=90.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        return run_reference(args)
+
+    world, rank, local, dist = dist_setup()
+    from nofluidx3d_gb300.core import CellSim
+
+    w = workloads.WORKLOADS[args.workload]()
+    mesh = w.mesh()
+    total = args.warmup + args.steps + args.profile_steps + args.e2e_steps + 200
+    sim = CellSim(local)
+    w.configure(sim, mesh, max_rows=total // w.record_every + 2)
+    nt, npn = mesh.num_tetra, mesh.num_points
+
+    # warm-up (also captures the CUDA graph)
+    sim.time_steps(args.warmup)
+    barrier(dist, local)
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms = sim.time_steps(args.steps)
+    barrier(dist, local)
+    clk = clocks.stop()
+    ms = reduce_max(dist, ms, local)
+    value = world * nt * args.steps / (ms / 1e3)
+
+    # per-kernel CUDA-event profile of the element and node passes
+    tet_ms, node_ms = sim.profile_steps(args.profile_steps)
+    tet_avg = tet_ms / args.profile_steps
+    elem_bytes = ELEM_BYTES[w.material] * nt
+    achieved = elem_bytes / (tet_avg / 1e3) / 1e9
+    peaks = load_peaks()
+    traffic_per_tet = load_traffic(args.workload)
+
+    # end to end through the C ABI with pinned host buffers
+    import torch
+
+    pos_host = torch.empty(3 * npn, dtype=torch.float64, pin_memory=True).numpy()
+    tab_host = torch.empty(w.record_every, dtype=torch.float64, pin_memory=True).numpy()
+    c = w.contacts()[w.record_contact]
+    intervals = max(1, args.e2e_steps // w.record_every)
+    barrier(dist, local)
+    sim.sync()
+    t0 = time.perf_counter()
+    for _ in range(intervals):
+        t = sim.time
+        tt = np.arange(t, t + w.record_every, dtype=np.float64)
+        tab_host[:] = c["p0"] - c["v"] * tt  # the host-side position callable
+        sim.set_contact_table(w.record_contact, t, tab_host)
+        sim.step(w.record_every)
+        sim.points_soa(out=pos_host)
+        _ = sim.curve()[-1]
+    sim.sync()
+    e2e_s = reduce_max(dist, time.perf_counter() - t0, local)
+    e2e_steps = intervals * w.record_every
+    e2e_val = world * nt * e2e_steps / e2e_s
+    h2d = 8.0 * w.record_every * intervals / e2e_steps + 16.0 / w.record_every
+    d2h = (8.0 * 3 * npn + 24.0) / w.record_every
+    status = sim.status()
+
+    if rank != 0:
+        sim.close()
+        barrier(dist, local)
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        try:
+            cpu = cpu_baseline(w, args.cpu_seconds)
+        except Exception as e:  # the baseline is reported, not required
+            cpu = {"value": None, "error": str(e)}
+    line = {
+        "metric": METRIC, "value": value, "unit": "tetra-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": w.name, "tets": nt, "nodes": npn, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": f"inputs larger than L2: {(ELEM_BYTES[w.material] * nt + NODE_BYTES * npn) / 1e6:.0f} MB "
+                         "of algorithmic state streamed per step vs 129 MB L2",
+                   "step_bytes_per_tetra": ELEM_BYTES[w.material] + NODE_BYTES * npn / nt,
+                   "step_gbs": (ELEM_BYTES[w.material] * nt + NODE_BYTES * npn) / (ms / args.steps / 1e3) / 1e9,
+                   "tet_pass_ms": tet_avg, "node_pass_ms": node_ms / args.profile_steps, "status": status},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
+                     "kernel": "k_tet_pass (element pass)",
+                     "algorithmic_bytes_per_launch": elem_bytes,
+                     "traffic": None if traffic_per_tet is None else traffic_per_tet * nt},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_val, "unit": "tetra-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": 2 * args.steps + (args.steps + 99) // 100,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    sim.close()
+    barrier(dist, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,178 @@
+/*
+ * nfx.h — C ABI of the GB300 implementation of noFluidX3D's explicit tetra-mesh time step.
+ *
+ * One nfx_sim handle is one cell simulation on one GPU: it owns the device buffers the
+ * reference's Simulation and its Interaction plugins own (nofluidx3d/Simulation.py:82-90,
+ * nofluidx3d/interactions/*.py createBuffers) and runs the whole step — element forces, node
+ * force accumulation, contacts, velocity Verlet, indenter-force readout — as CUDA kernels.
+ *
+ * Layout conventions are the reference's, so its Bridge host arrays (nofluidx3d/util/Bridge.py:16-26)
+ * can be passed as they are:
+ *   points / velocities / forces : double[3*np], SoA: x0..x_{np-1}, y0.., z0.. (Simulation.py:82-84)
+ *   tetras                       : uint32[4*nt], SoA: corner k of tetra t at [k*nt + t] (Simulation.py:85-87)
+ *   per-tetra fields             : double[nt]
+ * Internally nodes and tetrahedra are reordered for locality; every getter/setter converts.
+ *
+ * All functions return NFX_OK (0) or an NFX_ERR_* code; nfx_last_error() gives the message of
+ * the last failure on the calling thread. A handle must not be used from two threads at once.
+ * Steps are enqueued asynchronously on the handle's CUDA stream; getters synchronise.
+ */
+#ifndef NFX_H
+#define NFX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NFX_OK 0
+#define NFX_ERR_ARG 1       /* invalid argument (null pointer, size, index out of range, degenerate mesh) */
+#define NFX_ERR_CUDA 2      /* a CUDA runtime call failed (message has the CUDA error string) */
+#define NFX_ERR_STATE 3     /* call out of order, e.g. nfx_step before nfx_set_mesh */
+#define NFX_ERR_NOMEM 4     /* device allocation failed */
+#define NFX_ERR_NODEVICE 5  /* no CUDA device with the requested index */
+
+/* material models of nofluidx3d/interactions/Tetra.py:25-33 plus the viscoplastic law of
+ * nofluidx3d/kernels/InteractionFiniteStrainViscoplastic.cl */
+#define NFX_MODEL_MR 0   /* Mooney-Rivlin; Neo-Hookean is mooneyRivlinRatio = 1 (Tetra.py:77-78) */
+#define NFX_MODEL_SVK 1  /* Saint-Venant-Kirchhoff (tetra.cl:94-114) */
+#define NFX_MODEL_SVKK 2 /* Saint-Venant-Kirchhoff-Kellnberger (tetra.cl:76-93) */
+#define NFX_MODEL_VP 3   /* finite-strain viscoplastic (InteractionFiniteStrainViscoplastic.cl:1-220) */
+
+#define NFX_CONTACT_SUBSTRATE 0 /* nofluidx3d/interactions/Substrate.py, kernels/Interactions/Substrate.cl */
+#define NFX_CONTACT_PLANE 1     /* nofluidx3d/interactions/Plane.py, kernels/Interactions/Plane.cl */
+#define NFX_CONTACT_SPHERE 2    /* nofluidx3d/interactions/Sphere.py, kernels/Interactions/Sphere.cl */
+
+/* status bits (nfx_status) */
+#define NFX_STATUS_NONFINITE 1u  /* a position/velocity/force became NaN or Inf (util/IO.py:17-28 aborts on this) */
+#define NFX_STATUS_INVERTED 2u   /* an element reached det F <= 0 */
+#define NFX_STATUS_CURVE_FULL 4u /* a force-curve row fell outside the buffer given to nfx_set_record */
+
+/* per-tetra fields (nfx_get_tet_field) */
+#define NFX_FIELD_VON_MISES 0   /* vonMises buffer, Simulation.py:89 */
+#define NFX_FIELD_PRESSURE 1    /* pressure buffer, Simulation.py:90 (trace(sigma)/3, as the kernel writes it) */
+#define NFX_FIELD_PLASTIC_STRAIN 2 /* accumulatedStrain, Interactions.py:276 */
+
+typedef struct nfx_sim nfx_sim;
+
+/* Library version, e.g. 100 for 0.1.0. */
+int nfx_version(void);
+
+/* Copies the last error message of this thread into buf (NUL-terminated, truncated to len).
+ * Replaces the reference's print()+exit() error paths (openCL.py:30-32, util/IO.py:17-28). */
+int nfx_last_error(char* buf, size_t len);
+
+/* Creates a simulation on CUDA device `device`. Replaces initializeOpenCLObjects(gpu)
+ * (nofluidx3d/openCL.py:17-34): flat device index, one in-order stream. */
+int nfx_create(int device, nfx_sim** out);
+
+/* Frees all device and host resources of the handle. */
+int nfx_destroy(nfx_sim* sim);
+
+/* Uploads the cell mesh and resets the state (zero velocity, previous force and plastic state;
+ * time 0). Replaces the shared Bridges points/tetras of Simulation.__init__ (Simulation.py:65-90)
+ * plus the per-tetra reference quantities of Tetra.createBuffers (interactions/Tetra.py:49-64,
+ * TetraCell.py:33-41), which are computed here once. points: double[3*np] SoA (reference
+ * positions); tets: uint32[4*nt] SoA, positively oriented as tetra.cl:132 requires. */
+int nfx_set_mesh(nfx_sim* sim, int64_t np, int64_t nt, const double* points, const uint32_t* tets);
+
+/* Selects the elastic law with the reference's parameters: Tetra(cell, youngsModulus,
+ * poissonRatio, mooneyRivlinRatio, model) (interactions/Tetra.py:35-47; constants of
+ * tetra.cl:118-121). model: NFX_MODEL_MR / SVK / SVKK. */
+int nfx_set_tetra(nfx_sim* sim, int model, double youngs_modulus, double poisson_ratio, double mooney_rivlin_ratio);
+
+/* Selects the finite-strain viscoplastic law with uniform parameters
+ * par = {mu1, mu2, kappa, flowExponent, yieldStress, plasticFlowRate, hardeningThreshhold,
+ * hardeningExponent}: the constructor arguments of InteractionFiniteStrainViscoplastic
+ * (nofluidx3d/Interactions.py:257-277). Resets the plastic state to Fp = I, strain 0. */
+int nfx_set_viscoplastic(nfx_sim* sim, const double* par8);
+
+/* Adds a contact interaction; *id receives its index (0..3), which is also its order of
+ * application after the element force. position(t) = p0 - v*t while t <= tmove, then
+ * p0 - v*tmove (the wallFunc/sphereFunc schedules of Simulation.py:117-132, :173-183);
+ * substrate: position = p0. k is def_FORCE_CONST (Simulation.py:109, :134, :185).
+ * Replaces Substrate(wallPosition, k), Plane(wallFunc, k), Sphere(radius, sphereFunc, k). */
+int nfx_add_contact(nfx_sim* sim, int kind, double k, double radius, double p0, double v, double tmove, int* id);
+
+/* Supplies explicit per-step positions pos[0..n) for times t0..t0+n-1 of contact `id`,
+ * overriding its schedule; times outside the table use the nearest entry. This keeps
+ * arbitrary host callables working: the reference re-evaluates wallFunc(t) on the host every
+ * step in beforeTimeStep (interactions/Plane.py:39-41, Sphere.py:41-43). n = 0 removes it. */
+int nfx_set_contact_table(nfx_sim* sim, int id, int64_t t0, int64_t n, const double* pos);
+
+/* Velocity Verlet settings: damping xi (VelocityVerlet.cl:11 hard-codes 0.005) and the
+ * FIXED_TOP_BOTTOM pin of user nodes 3 and 4 (VelocityVerlet.cl:17-22,
+ * interactions/VelocityVerlet.py:23-45). */
+int nfx_set_integrator(nfx_sim* sim, double xi, int fix_top_bottom);
+
+/* Records the indenter force of contact `contact` every `every` steps into a device buffer of
+ * max_rows rows (t, indentation, force) — the recordedQuantities currentTime / indentationSI /
+ * forceSI of Simulation.py:94-100, :142-157, :194-216 in lattice units. Row r is time r*every.
+ * Per-tetra fields are refreshed on the same interval. contact = -1 disables recording. */
+int nfx_set_record(nfx_sim* sim, int contact, int64_t every, int64_t max_rows);
+
+/* Enqueues nsteps time steps (Simulation.timeStep, Simulation.py:232-237, nsteps times). */
+int nfx_step(nfx_sim* sim, int64_t nsteps);
+
+/* Computes the record row for the current time (when it is a record time) without stepping:
+ * the readout the reference makes after the last step of a run (Simulation.py:274-278). */
+int nfx_record_now(nfx_sim* sim);
+
+/* Waits for all enqueued work of the handle. */
+int nfx_sync(nfx_sim* sim);
+
+/* Current simulation time in steps (Simulation.time). */
+int nfx_get_time(nfx_sim* sim, int64_t* t);
+
+/* Node positions x = X + u, double[3*np] SoA in user order (Bridge.readFromGPU of points,
+ * util/IO.py:15). */
+int nfx_get_points(nfx_sim* sim, double* out);
+
+/* Overwrites node positions (Bridge.writeToGPU, util/Bridge.py:25-26). */
+int nfx_set_points(nfx_sim* sim, const double* in);
+
+/* Velocities, double[3*np] SoA (VelocityVerlet.velocityB, interactions/VelocityVerlet.py:29-33). */
+int nfx_get_velocities(nfx_sim* sim, double* out);
+int nfx_set_velocities(nfx_sim* sim, const double* in);
+
+/* Total force of the last step, double[3*np] SoA (VelocityVerlet.forceOldB). */
+int nfx_get_force_old(nfx_sim* sim, double* out);
+int nfx_set_force_old(nfx_sim* sim, const double* in);
+
+/* Per-tetra field in user tetra order (NFX_FIELD_*), double[nt]. */
+int nfx_get_tet_field(nfx_sim* sim, int which, double* out);
+
+/* Plastic deformation tensor Fp, double[9*nt] SoA (plasticDeformationTensor layout,
+ * Interactions.py:279-281). */
+int nfx_get_plastic_tensor(nfx_sim* sim, double* out);
+
+/* Copies the recorded rows (3 doubles each) into rows; *n_rows receives how many rows exist
+ * up to the current time (at most max_rows). */
+int nfx_get_curve(nfx_sim* sim, double* rows, int64_t max_rows, int64_t* n_rows);
+
+/* Indenter force of contact `contact` at the current time and positions, in lattice units:
+ * the forceSI closures (Simulation.py:146-153 plane, :198-212 sphere) without p0*L0^2. */
+int nfx_indenter_force(nfx_sim* sim, int contact, double* out);
+
+/* Device status bits (NFX_STATUS_*), accumulated since the last call with clear != 0. */
+int nfx_status(nfx_sim* sim, uint32_t* flags, int clear);
+
+/* Enqueues nsteps steps like nfx_step, bracketed by CUDA events recorded on the handle's
+ * stream, waits, and returns the elapsed device time in *ms. The reference only prints a
+ * wall-clock steps/s figure (Simulation.py:281-286). */
+int nfx_time_steps(nfx_sim* sim, int64_t nsteps, float* ms);
+
+/* Runs nsteps steps launch by launch with CUDA events around every kernel and returns the
+ * summed device time of the element passes (*tet_ms) and node passes (*node_ms). */
+int nfx_profile_steps(nfx_sim* sim, int64_t nsteps, float* tet_ms, float* node_ms);
+
+/* Number of mesh tiles and distinct-node entries (diagnostics for the tile layout). */
+int nfx_mesh_info(nfx_sim* sim, int64_t* ntiles, int64_t* tile_nodes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NFX_H */

@@ -1,0 +1,206 @@
+"""Thin Python handle over the C ABI: one `CellSim` is one nfx_sim (one cell on one GPU).
+
+Arrays cross the boundary in the reference's layouts (points/velocities SoA float64 3*Np,
+tetras SoA uint32 4*Nt); the convenience methods here accept and return (N, 3) / (Nt, 4)
+arrays and convert. Every call goes to libnfx; failures raise NfxError.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from typing import Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import (CONTACT_PLANE, CONTACT_SPHERE, CONTACT_SUBSTRATE, FIELD_PLASTIC_STRAIN, FIELD_PRESSURE,
+                   FIELD_VON_MISES, MODEL_MR, MODEL_SVK, MODEL_SVKK, MODEL_VP, NfxError, check)
+
+__all__ = ["CellSim", "NfxError", "MODEL_MR", "MODEL_SVK", "MODEL_SVKK", "MODEL_VP", "CONTACT_SUBSTRATE",
+           "CONTACT_PLANE", "CONTACT_SPHERE", "FIELD_VON_MISES", "FIELD_PRESSURE", "FIELD_PLASTIC_STRAIN",
+           "to_soa", "from_soa"]
+
+
+def to_soa(a: np.ndarray, dtype=np.float64) -> np.ndarray:
+    """(N, k) -> contiguous k*N SoA vector (the reference's order='F' reshape, Simulation.py:82-87)."""
+    a = np.asarray(a)
+    return np.ascontiguousarray(a.T.reshape(-1), dtype=dtype)
+
+
+def from_soa(v: np.ndarray, k: int) -> np.ndarray:
+    """k*N SoA vector -> (N, k)."""
+    return np.asarray(v).reshape(k, -1).T
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+class CellSim:
+    """One cell simulation on a CUDA device (see include/nfx.h for the semantics of each call)."""
+
+    def __init__(self, device: int = 0):
+        self._L = _lib.load()
+        h = C.c_void_p()
+        check(self._L.nfx_create(int(device), C.byref(h)))
+        self._h = h
+        self.device = device
+        self.np = 0
+        self.nt = 0
+        self.n_contacts = 0
+
+    # ------------------------------------------------------------------ lifecycle
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._L.nfx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ------------------------------------------------------------------ set-up
+    def set_mesh(self, points: np.ndarray, tets: np.ndarray) -> None:
+        pts = to_soa(points, np.float64)
+        tt = to_soa(tets, np.uint32)
+        np_, nt = int(np.asarray(points).shape[0]), int(np.asarray(tets).shape[0])
+        check(self._L.nfx_set_mesh(self._h, np_, nt, _ptr(pts), _ptr(tt)))
+        self.np, self.nt = np_, nt
+
+    def set_mesh_soa(self, np_: int, nt: int, points_soa: np.ndarray, tets_soa: np.ndarray) -> None:
+        pts = np.ascontiguousarray(points_soa, np.float64)
+        tt = np.ascontiguousarray(tets_soa, np.uint32)
+        check(self._L.nfx_set_mesh(self._h, int(np_), int(nt), _ptr(pts), _ptr(tt)))
+        self.np, self.nt = int(np_), int(nt)
+
+    def set_tetra(self, model: int, youngs: float, poisson: float, mr_ratio: float = 1.0) -> None:
+        check(self._L.nfx_set_tetra(self._h, int(model), float(youngs), float(poisson), float(mr_ratio)))
+
+    def set_viscoplastic(self, par: Sequence[float]) -> None:
+        p = np.ascontiguousarray(par, np.float64)
+        if p.size != 8:
+            raise ValueError("8 viscoplastic parameters expected")
+        check(self._L.nfx_set_viscoplastic(self._h, _ptr(p)))
+
+    def add_contact(self, kind: int, k: float, radius: float = 0.0, p0: float = 0.0, v: float = 0.0,
+                    tmove: float = float("inf")) -> int:
+        cid = C.c_int(-1)
+        check(self._L.nfx_add_contact(self._h, int(kind), float(k), float(radius), float(p0), float(v),
+                                      float(tmove), C.byref(cid)))
+        self.n_contacts += 1
+        return cid.value
+
+    def set_contact_table(self, cid: int, t0: int, positions: np.ndarray | None) -> None:
+        if positions is None or len(positions) == 0:
+            check(self._L.nfx_set_contact_table(self._h, int(cid), int(t0), 0, None))
+            return
+        p = np.ascontiguousarray(positions, np.float64)
+        check(self._L.nfx_set_contact_table(self._h, int(cid), int(t0), int(p.size), _ptr(p)))
+
+    def set_integrator(self, xi: float, fix_top_bottom: bool = False) -> None:
+        check(self._L.nfx_set_integrator(self._h, float(xi), int(bool(fix_top_bottom))))
+
+    def set_record(self, contact: int, every: int, max_rows: int) -> None:
+        check(self._L.nfx_set_record(self._h, int(contact), int(every), int(max_rows)))
+
+    # ------------------------------------------------------------------ stepping
+    def step(self, n: int = 1) -> None:
+        check(self._L.nfx_step(self._h, int(n)))
+
+    def record_now(self) -> None:
+        check(self._L.nfx_record_now(self._h))
+
+    def sync(self) -> None:
+        check(self._L.nfx_sync(self._h))
+
+    @property
+    def time(self) -> int:
+        t = C.c_int64()
+        check(self._L.nfx_get_time(self._h, C.byref(t)))
+        return t.value
+
+    # ------------------------------------------------------------------ state access
+    def _get3(self, fn) -> np.ndarray:
+        out = np.empty(3 * self.np, np.float64)
+        check(fn(self._h, _ptr(out)))
+        return out
+
+    def points_soa(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty(3 * self.np, np.float64)
+        check(self._L.nfx_get_points(self._h, _ptr(out)))
+        return out
+
+    def points(self) -> np.ndarray:
+        return from_soa(self.points_soa(), 3)
+
+    def set_points(self, pts: np.ndarray) -> None:
+        a = to_soa(pts) if np.asarray(pts).ndim == 2 else np.ascontiguousarray(pts, np.float64)
+        check(self._L.nfx_set_points(self._h, _ptr(a)))
+
+    def velocities(self) -> np.ndarray:
+        return from_soa(self._get3(self._L.nfx_get_velocities), 3)
+
+    def set_velocities(self, v: np.ndarray) -> None:
+        a = to_soa(v) if np.asarray(v).ndim == 2 else np.ascontiguousarray(v, np.float64)
+        check(self._L.nfx_set_velocities(self._h, _ptr(a)))
+
+    def force_old(self) -> np.ndarray:
+        return from_soa(self._get3(self._L.nfx_get_force_old), 3)
+
+    def set_force_old(self, f: np.ndarray) -> None:
+        a = to_soa(f) if np.asarray(f).ndim == 2 else np.ascontiguousarray(f, np.float64)
+        check(self._L.nfx_set_force_old(self._h, _ptr(a)))
+
+    def tet_field(self, which: int) -> np.ndarray:
+        out = np.empty(self.nt, np.float64)
+        check(self._L.nfx_get_tet_field(self._h, int(which), _ptr(out)))
+        return out
+
+    def plastic_tensor_soa(self) -> np.ndarray:
+        out = np.empty(9 * self.nt, np.float64)
+        check(self._L.nfx_get_plastic_tensor(self._h, _ptr(out)))
+        return out
+
+    def curve(self, max_rows: int = 1 << 20) -> np.ndarray:
+        n = C.c_int64()
+        check(self._L.nfx_get_curve(self._h, None, 0, C.byref(n)))
+        rows = min(n.value, max_rows)
+        out = np.zeros((max(rows, 1), 3), np.float64)
+        check(self._L.nfx_get_curve(self._h, _ptr(out), rows, C.byref(n)))
+        return out[:rows]
+
+    def indenter_force(self, contact: int) -> float:
+        out = C.c_double()
+        check(self._L.nfx_indenter_force(self._h, int(contact), C.byref(out)))
+        return out.value
+
+    def status(self, clear: bool = False) -> int:
+        f = C.c_uint32()
+        check(self._L.nfx_status(self._h, C.byref(f), int(bool(clear))))
+        return f.value
+
+    def time_steps(self, n: int) -> float:
+        """Run n steps; device milliseconds between CUDA events on the handle's stream."""
+        ms = C.c_float()
+        check(self._L.nfx_time_steps(self._h, int(n), C.byref(ms)))
+        return ms.value
+
+    def profile_steps(self, n: int) -> tuple[float, float]:
+        """Run n steps launch by launch; summed device ms of (element passes, node passes)."""
+        a, b = C.c_float(), C.c_float()
+        check(self._L.nfx_profile_steps(self._h, int(n), C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def mesh_info(self) -> tuple[int, int]:
+        a, b = C.c_int64(), C.c_int64()
+        check(self._L.nfx_mesh_info(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value

@@ -1,0 +1,692 @@
+// C ABI (include/nfx.h) of the GB300 tetra-mesh step: handle lifecycle, uploads, the step
+// loop (CUDA-graph chunks) and conversions between the user's layout and the device state.
+#include "../../include/nfx.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "nfx_internal.h"
+
+using namespace nfx;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+#define CUDA_TRY(expr)                                                                              \
+    do {                                                                                            \
+        cudaError_t e_ = (expr);                                                                    \
+        if (e_ != cudaSuccess) return fail(NFX_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+#define CHECK_ARG(cond, msg)                     \
+    do {                                         \
+        if (!(cond)) return fail(NFX_ERR_ARG, msg); \
+    } while (0)
+
+constexpr int GRAPH_STEPS = 100;  // steps per captured CUDA graph chunk
+
+}  // namespace
+
+struct nfx_sim {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool have_mesh = false;
+    bool have_material = false;
+    MeshPlan plan;
+    std::vector<void*> mesh_allocs;  // freed on re-mesh
+    MeshDev mesh{};
+    StateDev st{};
+    MaterialDev mat{};
+    StepParams prm{};
+    long long* d_node_user = nullptr;
+    double* d_stage = nullptr;
+    double* d_tables[MAX_CONTACTS] = {nullptr, nullptr, nullptr, nullptr};
+    long long* d_meta[MAX_CONTACTS] = {nullptr, nullptr, nullptr, nullptr};
+    long long table_cap[MAX_CONTACTS] = {0, 0, 0, 0};
+    // fixed-size control block
+    unsigned* d_status = nullptr;
+    long long* d_time = nullptr;
+    unsigned* d_counter = nullptr;
+    double* d_force_out = nullptr;
+    double* d_curve = nullptr;
+    long long curve_rows = 0;
+    long long rows_written = 0;  // rows recorded so far (row r is time r*every)
+    long long time = 0;          // host mirror of the device time
+    cudaGraphExec_t graph = nullptr;
+    bool graph_valid = false;
+};
+
+namespace {
+
+int set_device(nfx_sim* s) {
+    CUDA_TRY(cudaSetDevice(s->device));
+    return NFX_OK;
+}
+
+template <class T>
+int dalloc(nfx_sim* s, T** p, size_t count, std::vector<void*>* owner) {
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
+    if (e != cudaSuccess) return fail(NFX_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    *p = (T*)q;
+    if (owner) owner->push_back(q);
+    return NFX_OK;
+}
+
+void free_mesh(nfx_sim* s) {
+    for (void* p : s->mesh_allocs) cudaFree(p);
+    s->mesh_allocs.clear();
+    s->mesh = MeshDev{};
+    StateDev keep = s->st;
+    s->st = StateDev{};
+    s->st.status = keep.status;
+    s->st.time = keep.time;
+    s->st.counter = keep.counter;
+    s->st.force_out = keep.force_out;
+    s->st.curve = keep.curve;
+    s->d_node_user = nullptr;
+    s->d_stage = nullptr;
+    s->have_mesh = false;
+}
+
+void invalidate_graph(nfx_sim* s) {
+    if (s->graph) cudaGraphExecDestroy(s->graph);
+    s->graph = nullptr;
+    s->graph_valid = false;
+}
+
+int require_ready(nfx_sim* s) {
+    if (!s) return fail(NFX_ERR_ARG, "null handle");
+    if (!s->have_mesh) return fail(NFX_ERR_STATE, "no mesh: call nfx_set_mesh first");
+    if (!s->have_material) return fail(NFX_ERR_STATE, "no material: call nfx_set_tetra or nfx_set_viscoplastic first");
+    return NFX_OK;
+}
+
+int enqueue_steps(nfx_sim* s, int n) {
+    for (int k = 0; k < n; k++) {
+        CUDA_TRY(launch_tet_pass(s->mesh, s->st, s->mat, s->prm, k, s->stream));
+        CUDA_TRY(launch_node_pass(s->mesh, s->st, s->prm, k, NODE_UPDATE, -1, s->stream));
+    }
+    CUDA_TRY(launch_advance_time(s->st, n, s->stream));
+    return NFX_OK;
+}
+
+int build_graph(nfx_sim* s) {
+    invalidate_graph(s);
+    cudaGraph_t g = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_steps(s, GRAPH_STEPS);
+    cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+    if (rc != NFX_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return fail(NFX_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&s->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(NFX_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    s->graph_valid = true;
+    return NFX_OK;
+}
+
+void note_rows(nfx_sim* s, long long t_begin, long long t_end_inclusive) {
+    // rows produced by node passes at times in [t_begin, t_end_inclusive]
+    const long long every = s->prm.record_every;
+    if (s->prm.record_contact < 0 || every <= 0 || t_end_inclusive < t_begin) return;
+    const long long last = t_end_inclusive / every;  // last row index touched
+    if (last * every >= t_begin) s->rows_written = std::max(s->rows_written, std::min(last + 1, s->curve_rows));
+}
+
+}  // namespace
+
+extern "C" {
+
+int nfx_version(void) { return 100; }
+
+int nfx_last_error(char* buf, size_t len) {
+    if (!buf || len == 0) return NFX_ERR_ARG;
+    std::snprintf(buf, len, "%s", g_err.c_str());
+    return NFX_OK;
+}
+
+int nfx_create(int device, nfx_sim** out) {
+    if (!out) return fail(NFX_ERR_ARG, "out is null");
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0)
+        return fail(NFX_ERR_NODEVICE, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    if (device < 0 || device >= count)
+        return fail(NFX_ERR_NODEVICE, "device id " + std::to_string(device) + " does not exist (" +
+                                           std::to_string(count) + " devices)");
+    nfx_sim* s = new nfx_sim();
+    s->device = device;
+    int rc;
+    if ((rc = set_device(s)) != NFX_OK) { delete s; return rc; }
+    e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete s; return fail(NFX_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)); }
+    if ((rc = dalloc(s, &s->d_status, 1, nullptr)) != NFX_OK || (rc = dalloc(s, &s->d_time, 1, nullptr)) != NFX_OK ||
+        (rc = dalloc(s, &s->d_counter, 1, nullptr)) != NFX_OK || (rc = dalloc(s, &s->d_force_out, 1, nullptr)) != NFX_OK) {
+        nfx_destroy(s);
+        return rc;
+    }
+    cudaMemsetAsync(s->d_status, 0, sizeof(unsigned), s->stream);
+    cudaMemsetAsync(s->d_time, 0, sizeof(long long), s->stream);
+    cudaMemsetAsync(s->d_counter, 0, sizeof(unsigned), s->stream);
+    s->st.status = s->d_status;
+    s->st.time = s->d_time;
+    s->st.counter = s->d_counter;
+    s->st.force_out = s->d_force_out;
+    s->prm.record_contact = -1;
+    s->prm.fix_a = s->prm.fix_b = -1;
+    // default integrator: the reference's xi = 0.005 (VelocityVerlet.cl:11)
+    const double xi = 0.005;
+    s->prm.vv_a = (float)((1 - 0.5 * xi) / (1 + 0.5 * xi));
+    s->prm.vv_hb = (float)(0.5 / (1 + 0.5 * xi));
+    s->prm.vv_dm = (float)(1 - 0.5 * xi);
+    *out = s;
+    return NFX_OK;
+}
+
+int nfx_destroy(nfx_sim* s) {
+    if (!s) return NFX_OK;
+    cudaSetDevice(s->device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    invalidate_graph(s);
+    free_mesh(s);
+    for (int c = 0; c < MAX_CONTACTS; c++) {
+        if (s->d_tables[c]) cudaFree(s->d_tables[c]);
+        if (s->d_meta[c]) cudaFree(s->d_meta[c]);
+    }
+    if (s->d_curve) cudaFree(s->d_curve);
+    if (s->d_status) cudaFree(s->d_status);
+    if (s->d_time) cudaFree(s->d_time);
+    if (s->d_counter) cudaFree(s->d_counter);
+    if (s->d_force_out) cudaFree(s->d_force_out);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return NFX_OK;
+}
+
+int nfx_set_mesh(nfx_sim* s, int64_t np, int64_t nt, const double* points, const uint32_t* tets) {
+    CHECK_ARG(s, "null handle");
+    CHECK_ARG(points && tets, "null points or tets");
+    int rc;
+    if ((rc = set_device(s)) != NFX_OK) return rc;
+    MeshPlan plan;
+    std::string err;
+    if (!build_mesh_plan(np, nt, points, tets, plan, err)) return fail(NFX_ERR_ARG, err);
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    invalidate_graph(s);
+    free_mesh(s);
+    s->plan = std::move(plan);
+    const MeshPlan& P = s->plan;
+    auto& A = s->mesh_allocs;
+    int* tb; int* nbg; unsigned* tn; uchar4* lc; float4 *da, *db; float2* dc; float4 *xh, *xl;
+    float4 *uh, *ul, *v, *fo, *fa; double* part;
+    if ((rc = dalloc(s, &tb, P.tile_tet_begin.size(), &A)) || (rc = dalloc(s, &nbg, P.tile_node_begin.size(), &A)) ||
+        (rc = dalloc(s, &tn, P.tile_nodes.size(), &A)) || (rc = dalloc(s, &lc, (size_t)nt, &A)) ||
+        (rc = dalloc(s, &da, (size_t)nt, &A)) || (rc = dalloc(s, &db, (size_t)nt, &A)) || (rc = dalloc(s, &dc, (size_t)nt, &A)) ||
+        (rc = dalloc(s, &xh, (size_t)np, &A)) || (rc = dalloc(s, &xl, (size_t)np, &A)) || (rc = dalloc(s, &uh, (size_t)np, &A)) ||
+        (rc = dalloc(s, &ul, (size_t)np, &A)) || (rc = dalloc(s, &v, (size_t)np, &A)) || (rc = dalloc(s, &fo, (size_t)np, &A)) ||
+        (rc = dalloc(s, &fa, (size_t)np, &A)) || (rc = dalloc(s, &part, (size_t)((np + NODE_BLOCK - 1) / NODE_BLOCK), &A)) ||
+        (rc = dalloc(s, &s->d_node_user, (size_t)np, &A)) || (rc = dalloc(s, &s->d_stage, 9 * (size_t)std::max(np, nt), &A))) {
+        free_mesh(s);
+        return rc;
+    }
+    // per-tetra constants, split into the float4/float4/float2 streams the kernel reads
+    std::vector<float> a(4 * (size_t)nt), b(4 * (size_t)nt), c(2 * (size_t)nt);
+    for (int64_t t = 0; t < nt; t++) {
+        const float* o = &P.dmi[12 * t];
+        for (int k = 0; k < 4; k++) a[4 * t + k] = o[k];
+        for (int k = 0; k < 4; k++) b[4 * t + k] = o[4 + k];
+        c[2 * t] = o[8];
+        c[2 * t + 1] = o[9];
+    }
+    std::vector<long long> nu(P.node_user.begin(), P.node_user.end());
+    cudaStream_t st = s->stream;
+    CUDA_TRY(cudaMemcpyAsync(tb, P.tile_tet_begin.data(), P.tile_tet_begin.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(nbg, P.tile_node_begin.data(), P.tile_node_begin.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(tn, P.tile_nodes.data(), P.tile_nodes.size() * sizeof(unsigned), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(lc, P.lconn.data(), P.lconn.size(), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(da, a.data(), a.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(db, b.data(), b.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(dc, c.data(), c.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(xh, P.Xh.data(), P.Xh.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(xl, P.Xl.data(), P.Xl.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(s->d_node_user, nu.data(), nu.size() * sizeof(long long), cudaMemcpyHostToDevice, st));
+    for (float4* z : {uh, ul, v, fo, fa}) CUDA_TRY(cudaMemsetAsync(z, 0, (size_t)np * sizeof(float4), st));
+    CUDA_TRY(cudaMemsetAsync(s->d_time, 0, sizeof(long long), st));
+    CUDA_TRY(cudaMemsetAsync(s->d_status, 0, sizeof(unsigned), st));
+    CUDA_TRY(cudaStreamSynchronize(st));  // host vectors a/b/c/nu go out of scope
+    s->mesh.np = (int)np;
+    s->mesh.nt = (int)nt;
+    s->mesh.ntiles = (int)P.ntiles;
+    s->mesh.tile_tet_begin = tb;
+    s->mesh.tile_node_begin = nbg;
+    s->mesh.tile_nodes = tn;
+    s->mesh.lconn = lc;
+    s->mesh.dmi_a = da;
+    s->mesh.dmi_b = db;
+    s->mesh.dmi_c = dc;
+    s->mesh.Xh = xh;
+    s->mesh.Xl = xl;
+    s->st.uh = uh;
+    s->st.ul = ul;
+    s->st.v = v;
+    s->st.fo = fo;
+    s->st.facc = fa;
+    s->st.partials = part;
+    s->time = 0;
+    s->rows_written = 0;
+    s->prm.fix_a = s->prm.fix_b = -1;
+    s->have_mesh = true;
+    // the viscoplastic state follows the mesh
+    if (s->have_material && s->mat.model == MODEL_VP) {
+        s->have_material = false;
+        return fail(NFX_ERR_STATE, "mesh replaced: call nfx_set_viscoplastic again");
+    }
+    return NFX_OK;
+}
+
+int nfx_set_tetra(nfx_sim* s, int model, double E, double nu, double mr) {
+    CHECK_ARG(s, "null handle");
+    CHECK_ARG(model == NFX_MODEL_MR || model == NFX_MODEL_SVK || model == NFX_MODEL_SVKK, "unknown elastic model");
+    CHECK_ARG(std::isfinite(E) && std::isfinite(nu) && std::isfinite(mr), "non-finite material parameter");
+    CHECK_ARG(nu != 0.5, "poisson ratio 0.5 makes the bulk modulus infinite");
+    // constants of tetra.cl:79-84, :97-102, :118-121
+    const double mu = E / (2 * (1 + nu));
+    s->mat = MaterialDev{};
+    s->mat.model = model;
+    s->mat.mu1 = (float)(mr * mu);
+    s->mat.mu2 = (float)((1 - mr) * mu);
+    s->mat.kappa = (float)(E / (3 * (1 - 2 * nu)));
+    s->mat.mu = (float)mu;
+    s->mat.kp = (float)(nu / (1 - 2 * nu));
+    s->have_material = true;
+    invalidate_graph(s);
+    return NFX_OK;
+}
+
+int nfx_set_viscoplastic(nfx_sim* s, const double* par) {
+    CHECK_ARG(s && par, "null argument");
+    if (!s->have_mesh) return fail(NFX_ERR_STATE, "no mesh: call nfx_set_mesh first");
+    for (int k = 0; k < 8; k++) CHECK_ARG(std::isfinite(par[k]), "non-finite viscoplastic parameter");
+    CHECK_ARG(par[4] > 0, "yield stress must be positive");
+    CHECK_ARG(par[6] != 0, "hardening threshold must be non-zero");
+    int rc;
+    if ((rc = set_device(s)) != NFX_OK) return rc;
+    const int64_t nt = s->plan.nt;
+    if (!s->st.vp_a) {
+        if ((rc = dalloc(s, &s->st.vp_a, (size_t)nt, &s->mesh_allocs)) || (rc = dalloc(s, &s->st.vp_b, (size_t)nt, &s->mesh_allocs)) ||
+            (rc = dalloc(s, &s->st.vp_c, (size_t)nt, &s->mesh_allocs)) || (rc = dalloc(s, &s->st.fields, (size_t)nt, &s->mesh_allocs)))
+            return rc;
+    }
+    CUDA_TRY(cudaMemsetAsync(s->st.vp_a, 0, (size_t)nt * sizeof(float4), s->stream));
+    CUDA_TRY(cudaMemsetAsync(s->st.vp_b, 0, (size_t)nt * sizeof(float4), s->stream));
+    CUDA_TRY(cudaMemsetAsync(s->st.vp_c, 0, (size_t)nt * sizeof(float2), s->stream));
+    CUDA_TRY(cudaMemsetAsync(s->st.fields, 0, (size_t)nt * sizeof(float2), s->stream));
+    s->mat = MaterialDev{};
+    s->mat.model = MODEL_VP;
+    s->mat.mu1 = (float)par[0];
+    s->mat.mu2 = (float)par[1];
+    s->mat.kappa = (float)par[2];
+    s->mat.flow_exp = (float)par[3];
+    s->mat.yield = (float)par[4];
+    s->mat.flow_rate = (float)par[5];
+    s->mat.hard_thr = (float)par[6];
+    s->mat.hard_exp = (float)par[7];
+    s->have_material = true;
+    invalidate_graph(s);
+    return NFX_OK;
+}
+
+int nfx_add_contact(nfx_sim* s, int kind, double k, double radius, double p0, double v, double tmove, int* id) {
+    CHECK_ARG(s, "null handle");
+    CHECK_ARG(kind == NFX_CONTACT_SUBSTRATE || kind == NFX_CONTACT_PLANE || kind == NFX_CONTACT_SPHERE, "unknown contact kind");
+    CHECK_ARG(s->prm.n_contacts < MAX_CONTACTS, "at most 4 contacts");
+    CHECK_ARG(std::isfinite(k) && std::isfinite(p0) && std::isfinite(v) && !std::isnan(tmove), "non-finite contact parameter");
+    CHECK_ARG(kind != NFX_CONTACT_SPHERE || radius > 0, "sphere radius must be positive");
+    int rc;
+    if ((rc = set_device(s)) != NFX_OK) return rc;
+    const int i = s->prm.n_contacts;
+    if (!s->d_meta[i] && (rc = dalloc(s, &s->d_meta[i], 2, nullptr)) != NFX_OK) return rc;
+    CUDA_TRY(cudaMemsetAsync(s->d_meta[i], 0, 2 * sizeof(long long), s->stream));
+    ContactDev c{};
+    c.kind = kind;
+    c.k = k;
+    c.radius = radius;
+    c.p0 = p0;
+    c.v = v;
+    c.tmove = tmove;
+    c.table = s->d_tables[i];
+    c.meta = s->d_meta[i];
+    s->prm.c[i] = c;
+    s->prm.n_contacts++;
+    if (id) *id = i;
+    invalidate_graph(s);
+    return NFX_OK;
+}
+
+int nfx_set_contact_table(nfx_sim* s, int id, int64_t t0, int64_t n, const double* pos) {
+    CHECK_ARG(s, "null handle");
+    CHECK_ARG(id >= 0 && id < s->prm.n_contacts, "contact id out of range");
+    CHECK_ARG(n >= 0 && (n == 0 || pos), "bad table");
+    for (int64_t k = 0; k < n; k++) CHECK_ARG(std::isfinite(pos[k]), "non-finite table position");
+    int rc;
+    if ((rc = set_device(s)) != NFX_OK) return rc;
+    // steps already enqueued may still read the table: wait, then refill in stream order
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    if (n > s->table_cap[id]) {
+        if (s->d_tables[id]) cudaFree(s->d_tables[id]);
+        s->d_tables[id] = nullptr;
+        s->table_cap[id] = 0;
+        const long long cap = std::max<long long>(n, 4096);
+        if ((rc = dalloc(s, &s->d_tables[id], (size_t)cap, nullptr)) != NFX_OK) return rc;
+        s->table_cap[id] = cap;
+        s->prm.c[id].table = s->d_tables[id];
+        invalidate_graph(s);  // the table pointer is a kernel parameter
+    }
+    const long long meta[2] = {(long long)t0, (long long)n};
+    if (n > 0) CUDA_TRY(cudaMemcpyAsync(s->d_tables[id], pos, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(cudaMemcpyAsync(s->d_meta[id], meta, sizeof(meta), cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return NFX_OK;
+}
+
+int nfx_set_integrator(nfx_sim* s, double xi, int fix_top_bottom) {
+    CHECK_ARG(s, "null handle");
+    CHECK_ARG(std::isfinite(xi) && xi > -2.0, "bad damping");
+    // v' = (v (1 - xi/2) + (f + fo)/2) / (1 + xi/2);  x' = x + v'(1 - xi/2) + f/2  (VelocityVerlet.cl:12-14)
+    s->prm.vv_a = (float)((1 - 0.5 * xi) / (1 + 0.5 * xi));
+    s->prm.vv_hb = (float)(0.5 / (1 + 0.5 * xi));
+    s->prm.vv_dm = (float)(1 - 0.5 * xi);
+    s->prm.fix_a = s->prm.fix_b = -1;
+    if (fix_top_bottom) {
+        if (!s->have_mesh) return fail(NFX_ERR_STATE, "set the mesh before pinning nodes 3 and 4");
+        if (s->plan.np > 3) s->prm.fix_a = (int)s->plan.node_int[3];
+        if (s->plan.np > 4) s->prm.fix_b = (int)s->plan.node_int[4];
+    }
+    invalidate_graph(s);
+    return NFX_OK;
+}
+
+int nfx_set_record(nfx_sim* s, int contact, int64_t every, int64_t max_rows) {
+    CHECK_ARG(s, "null handle");
+    CHECK_ARG(contact >= -1 && contact < s->prm.n_contacts, "contact id out of range");
+    CHECK_ARG(contact < 0 || (every > 0 && max_rows > 0), "every and max_rows must be positive");
+    int rc;
+    if ((rc = set_device(s)) != NFX_OK) return rc;
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    if (contact >= 0 && max_rows > s->curve_rows) {
+        if (s->d_curve) cudaFree(s->d_curve);
+        s->d_curve = nullptr;
+        s->curve_rows = 0;
+        if ((rc = dalloc(s, &s->d_curve, 3 * (size_t)max_rows, nullptr)) != NFX_OK) return rc;
+        s->curve_rows = max_rows;
+    }
+    if (s->d_curve) CUDA_TRY(cudaMemsetAsync(s->d_curve, 0, 3 * (size_t)s->curve_rows * sizeof(double), s->stream));
+    s->st.curve = s->d_curve;
+    s->prm.record_contact = contact;
+    s->prm.record_every = contact >= 0 ? every : 0;
+    s->prm.max_rows = contact >= 0 ? max_rows : 0;
+    s->prm.fields_every = contact >= 0 ? every : 0;
+    s->rows_written = 0;
+    invalidate_graph(s);
+    return NFX_OK;
+}
+
+int nfx_step(nfx_sim* s, int64_t nsteps) {
+    int rc;
+    if ((rc = require_ready(s)) != NFX_OK) return rc;
+    CHECK_ARG(nsteps >= 0, "negative step count");
+    if ((rc = set_device(s)) != NFX_OK) return rc;
+    const long long t_begin = s->time;
+    int64_t left = nsteps;
+    while (left >= GRAPH_STEPS) {
+        if (!s->graph_valid && (rc = build_graph(s)) != NFX_OK) return rc;
+        CUDA_TRY(cudaGraphLaunch(s->graph, s->stream));
+        left -= GRAPH_STEPS;
+    }
+    if (left > 0 && (rc = enqueue_steps(s, (int)left)) != NFX_OK) return rc;
+    s->time += nsteps;
+    if (nsteps > 0) note_rows(s, t_begin, s->time - 1);
+    return NFX_OK;
+}
+
+int nfx_record_now(nfx_sim* s) {
+    int rc;
+    if ((rc = require_ready(s)) != NFX_OK) return rc;
+    if ((rc = set_device(s)) != NFX_OK) return rc;
+    if (s->prm.record_contact < 0) return NFX_OK;
+    CUDA_TRY(launch_node_pass(s->mesh, s->st, s->prm, 0, NODE_READOUT_ROW, -1, s->stream));
+    note_rows(s, s->time, s->time);
+    return NFX_OK;
+}
+
+int nfx_sync(nfx_sim* s) {
+    CHECK_ARG(s, "null handle");
+    int rc;
+    if ((rc = set_device(s)) != NFX_OK) return rc;
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return NFX_OK;
+}
+
+int nfx_get_time(nfx_sim* s, int64_t* t) {
+    CHECK_ARG(s && t, "null argument");
+    *t = s->time;
+    return NFX_OK;
+}
+
+int nfx_get_points(nfx_sim* s, double* out) {
+    CHECK_ARG(s && out, "null argument");
+    if (!s->have_mesh) return fail(NFX_ERR_STATE, "no mesh");
+    int rc;
+    if ((rc = set_device(s)) != NFX_OK) return rc;
+    CUDA_TRY(launch_points_to_user(s->mesh, s->st, s->d_node_user, s->d_stage, s->stream));
+    CUDA_TRY(cudaMemcpyAsync(out, s->d_stage, 3 * (size_t)s->plan.np * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return NFX_OK;
+}
+
+int nfx_set_points(nfx_sim* s, const double* in) {
+    CHECK_ARG(s && in, "null argument");
+    if (!s->have_mesh) return fail(NFX_ERR_STATE, "no mesh");
+    int rc;
+    if ((rc = set_device(s)) != NFX_OK) return rc;
+    CUDA_TRY(cudaMemcpyAsync(s->d_stage, in, 3 * (size_t)s->plan.np * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(launch_points_from_user(s->mesh, s->st, s->d_node_user, s->d_stage, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return NFX_OK;
+}
+
+static int get_vec(nfx_sim* s, float4* a, double* out) {
+    CHECK_ARG(s && out, "null argument");
+    if (!s->have_mesh) return fail(NFX_ERR_STATE, "no mesh");
+    int rc;
+    if ((rc = set_device(s)) != NFX_OK) return rc;
+    CUDA_TRY(launch_vec_to_user(s->mesh, a, s->d_node_user, s->d_stage, s->stream));
+    CUDA_TRY(cudaMemcpyAsync(out, s->d_stage, 3 * (size_t)s->plan.np * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return NFX_OK;
+}
+
+static int set_vec(nfx_sim* s, float4* a, const double* in) {
+    CHECK_ARG(s && in, "null argument");
+    if (!s->have_mesh) return fail(NFX_ERR_STATE, "no mesh");
+    int rc;
+    if ((rc = set_device(s)) != NFX_OK) return rc;
+    CUDA_TRY(cudaMemcpyAsync(s->d_stage, in, 3 * (size_t)s->plan.np * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(launch_vec_from_user(s->mesh, a, s->d_node_user, s->d_stage, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return NFX_OK;
+}
+
+int nfx_get_velocities(nfx_sim* s, double* out) { return s ? get_vec(s, s->st.v, out) : fail(NFX_ERR_ARG, "null handle"); }
+int nfx_set_velocities(nfx_sim* s, const double* in) { return s ? set_vec(s, s->st.v, in) : fail(NFX_ERR_ARG, "null handle"); }
+int nfx_get_force_old(nfx_sim* s, double* out) { return s ? get_vec(s, s->st.fo, out) : fail(NFX_ERR_ARG, "null handle"); }
+int nfx_set_force_old(nfx_sim* s, const double* in) { return s ? set_vec(s, s->st.fo, in) : fail(NFX_ERR_ARG, "null handle"); }
+
+int nfx_get_tet_field(nfx_sim* s, int which, double* out) {
+    CHECK_ARG(s && out, "null argument");
+    CHECK_ARG(which >= 0 && which <= 2, "unknown field");
+    if (!s->have_mesh) return fail(NFX_ERR_STATE, "no mesh");
+    const int64_t nt = s->plan.nt;
+    if (s->mat.model != MODEL_VP || !s->st.vp_c) {
+        // the elastic kernel (tetra.cl) writes no per-tetra fields; the reference's buffers stay 0
+        std::fill(out, out + nt, 0.0);
+        return NFX_OK;
+    }
+    int rc;
+    if ((rc = set_device(s)) != NFX_OK) return rc;
+    std::vector<float> h(2 * (size_t)nt);
+    const float2* src = which == 2 ? s->st.vp_c : s->st.fields;
+    CUDA_TRY(cudaMemcpyAsync(h.data(), src, (size_t)nt * sizeof(float2), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    const int comp = which == 0 ? 0 : 1;
+    for (int64_t t = 0; t < nt; t++) out[s->plan.tet_user[t]] = (double)h[2 * t + comp];
+    return NFX_OK;
+}
+
+int nfx_get_plastic_tensor(nfx_sim* s, double* out) {
+    CHECK_ARG(s && out, "null argument");
+    if (!s->have_mesh) return fail(NFX_ERR_STATE, "no mesh");
+    const int64_t nt = s->plan.nt;
+    if (s->mat.model != MODEL_VP || !s->st.vp_a) {
+        for (int k = 0; k < 9; k++)
+            for (int64_t t = 0; t < nt; t++) out[k * nt + t] = (k % 4 == 0) ? 1.0 : 0.0;
+        return NFX_OK;
+    }
+    int rc;
+    if ((rc = set_device(s)) != NFX_OK) return rc;
+    std::vector<float> a(4 * (size_t)nt), b(4 * (size_t)nt), c(2 * (size_t)nt);
+    CUDA_TRY(cudaMemcpyAsync(a.data(), s->st.vp_a, (size_t)nt * sizeof(float4), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaMemcpyAsync(b.data(), s->st.vp_b, (size_t)nt * sizeof(float4), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaMemcpyAsync(c.data(), s->st.vp_c, (size_t)nt * sizeof(float2), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    for (int64_t t = 0; t < nt; t++) {
+        const int64_t u = s->plan.tet_user[t];
+        const float P[9] = {a[4 * t], a[4 * t + 1], a[4 * t + 2], a[4 * t + 3], b[4 * t], b[4 * t + 1],
+                            b[4 * t + 2], b[4 * t + 3], c[2 * t]};
+        for (int k = 0; k < 9; k++) out[k * nt + u] = (double)P[k] + ((k % 4 == 0) ? 1.0 : 0.0);
+    }
+    return NFX_OK;
+}
+
+int nfx_get_curve(nfx_sim* s, double* rows, int64_t max_rows, int64_t* n_rows) {
+    CHECK_ARG(s && n_rows, "null argument");
+    CHECK_ARG(max_rows >= 0 && (max_rows == 0 || rows), "bad row buffer");
+    int rc;
+    if ((rc = set_device(s)) != NFX_OK) return rc;
+    const long long n = std::min<long long>(s->rows_written, max_rows);
+    if (n > 0) {
+        CUDA_TRY(cudaMemcpyAsync(rows, s->d_curve, 3 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    }
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    *n_rows = s->rows_written;
+    return NFX_OK;
+}
+
+int nfx_indenter_force(nfx_sim* s, int contact, double* out) {
+    int rc;
+    if ((rc = require_ready(s)) != NFX_OK) return rc;
+    CHECK_ARG(out, "null out");
+    CHECK_ARG(contact >= 0 && contact < s->prm.n_contacts, "contact id out of range");
+    if ((rc = set_device(s)) != NFX_OK) return rc;
+    CUDA_TRY(launch_node_pass(s->mesh, s->st, s->prm, 0, NODE_READOUT_VALUE, contact, s->stream));
+    CUDA_TRY(cudaMemcpyAsync(out, s->d_force_out, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return NFX_OK;
+}
+
+int nfx_status(nfx_sim* s, uint32_t* flags, int clear) {
+    CHECK_ARG(s && flags, "null argument");
+    int rc;
+    if ((rc = set_device(s)) != NFX_OK) return rc;
+    unsigned h = 0;
+    CUDA_TRY(cudaMemcpyAsync(&h, s->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, s->stream));
+    if (clear) CUDA_TRY(cudaMemsetAsync(s->d_status, 0, sizeof(unsigned), s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    *flags = h;
+    return NFX_OK;
+}
+
+int nfx_time_steps(nfx_sim* s, int64_t nsteps, float* ms) {
+    CHECK_ARG(s && ms, "null argument");
+    int rc;
+    if ((rc = require_ready(s)) != NFX_OK) return rc;
+    if ((rc = set_device(s)) != NFX_OK) return rc;
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    CUDA_TRY(cudaEventRecord(e0, s->stream));
+    rc = nfx_step(s, nsteps);
+    cudaEventRecord(e1, s->stream);
+    cudaError_t e = cudaEventSynchronize(e1);
+    float t = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != NFX_OK) return rc;
+    if (e != cudaSuccess) return fail(NFX_ERR_CUDA, std::string("event timing: ") + cudaGetErrorString(e));
+    *ms = t;
+    return NFX_OK;
+}
+
+int nfx_profile_steps(nfx_sim* s, int64_t nsteps, float* tet_ms, float* node_ms) {
+    CHECK_ARG(s && tet_ms && node_ms, "null argument");
+    CHECK_ARG(nsteps >= 0 && nsteps <= (1 << 20), "bad step count");
+    int rc;
+    if ((rc = require_ready(s)) != NFX_OK) return rc;
+    if ((rc = set_device(s)) != NFX_OK) return rc;
+    std::vector<cudaEvent_t> ev(3 * (size_t)nsteps + 1);
+    for (auto& e : ev) CUDA_TRY(cudaEventCreate(&e));
+    const long long t_begin = s->time;
+    cudaError_t err = cudaSuccess;
+    for (int64_t k = 0; k < nsteps && err == cudaSuccess; k++) {
+        cudaEventRecord(ev[3 * k], s->stream);
+        err = launch_tet_pass(s->mesh, s->st, s->mat, s->prm, (int)k, s->stream);
+        cudaEventRecord(ev[3 * k + 1], s->stream);
+        if (err == cudaSuccess) err = launch_node_pass(s->mesh, s->st, s->prm, (int)k, NODE_UPDATE, -1, s->stream);
+        cudaEventRecord(ev[3 * k + 2], s->stream);
+    }
+    if (err == cudaSuccess) err = launch_advance_time(s->st, nsteps, s->stream);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s->stream);
+    float a = 0.f, b = 0.f;
+    for (int64_t k = 0; k < nsteps && err == cudaSuccess; k++) {
+        float x = 0.f, y = 0.f;
+        err = cudaEventElapsedTime(&x, ev[3 * k], ev[3 * k + 1]);
+        if (err == cudaSuccess) err = cudaEventElapsedTime(&y, ev[3 * k + 1], ev[3 * k + 2]);
+        a += x;
+        b += y;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    if (err != cudaSuccess) return fail(NFX_ERR_CUDA, std::string("profile_steps: ") + cudaGetErrorString(err));
+    s->time += nsteps;
+    if (nsteps > 0) note_rows(s, t_begin, s->time - 1);
+    *tet_ms = a;
+    *node_ms = b;
+    return NFX_OK;
+}
+
+int nfx_mesh_info(nfx_sim* s, int64_t* ntiles, int64_t* tile_nodes) {
+    CHECK_ARG(s && ntiles && tile_nodes, "null argument");
+    if (!s->have_mesh) return fail(NFX_ERR_STATE, "no mesh");
+    *ntiles = s->plan.ntiles;
+    *tile_nodes = (int64_t)s->plan.tile_nodes.size();
+    return NFX_OK;
+}
+
+}  // extern "C"

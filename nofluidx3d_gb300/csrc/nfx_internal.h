@@ -1,0 +1,131 @@
+// Internal data structures shared by the host runtime (nfx_api.cpp, nfx_mesh.cpp) and the
+// kernels (nfx_kernels.cu). Not part of the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace nfx {
+
+enum Model : int { MODEL_MR = 0, MODEL_SVK = 1, MODEL_SVKK = 2, MODEL_VP = 3 };
+enum ContactKind : int { CONTACT_SUBSTRATE = 0, CONTACT_PLANE = 1, CONTACT_SPHERE = 2 };
+
+constexpr int MAX_CONTACTS = 4;
+// A tile is a run of consecutive tetrahedra (after reordering) processed by one CTA. Its
+// distinct nodes are listed once, so the per-tetra connectivity is four 8-bit local indices
+// and the tile's nodal forces are summed in shared memory before one flush per node.
+constexpr int TILE_TETS = 256;
+constexpr int TILE_NODES_MAX = 256;
+constexpr int NODE_BLOCK = 256;
+
+// Status bits raised by the kernels (read back by nfx_status).
+constexpr unsigned STATUS_NONFINITE = 1u;   // a position or force became NaN/Inf
+constexpr unsigned STATUS_INVERTED = 2u;    // an element reached det F <= 0
+constexpr unsigned STATUS_CURVE_FULL = 4u;  // a record row fell outside the curve buffer
+
+// ---------------------------------------------------------------------------------------
+// Host-side mesh plan: reordering, tiles, per-tetra reference quantities.
+// ---------------------------------------------------------------------------------------
+struct MeshPlan {
+    int64_t np = 0, nt = 0, ntiles = 0;
+    std::vector<int64_t> node_user;   // internal node -> user node id
+    std::vector<int64_t> node_int;    // user node id -> internal node
+    std::vector<int64_t> tet_user;    // internal tetra -> user tetra id
+    std::vector<int32_t> tile_tet_begin;   // ntiles + 1
+    std::vector<int32_t> tile_node_begin;  // ntiles + 1
+    std::vector<uint32_t> tile_nodes;      // internal node ids, sorted within a tile
+    std::vector<uint8_t> lconn;            // 4 * nt local corner indices (internal tet order)
+    std::vector<float> dmi;                // 12 * nt: Dm^-1 row-major (9), V0, pad, pad
+    std::vector<float> Xh, Xl;             // 4 * np: reference position hi / lo parts
+};
+
+// Builds the plan from the reference's layouts (points SoA 3*np doubles, tets SoA 4*nt).
+// Returns false with a message on invalid input (index out of range, degenerate tetra).
+bool build_mesh_plan(int64_t np, int64_t nt, const double* points_soa, const uint32_t* tets_soa, MeshPlan& plan,
+                     std::string& err);
+
+// ---------------------------------------------------------------------------------------
+// Device views passed to kernels by value.
+// ---------------------------------------------------------------------------------------
+struct MeshDev {
+    int np, nt, ntiles;
+    const int* tile_tet_begin;
+    const int* tile_node_begin;
+    const unsigned* tile_nodes;
+    const uchar4* lconn;
+    const float4* dmi_a;  // Dm^-1 entries 0..3
+    const float4* dmi_b;  // Dm^-1 entries 4..7
+    const float2* dmi_c;  // Dm^-1 entry 8, V0
+    const float4* Xh;
+    const float4* Xl;
+};
+
+struct StateDev {
+    float4* uh;     // displacement hi
+    float4* ul;     // displacement lo
+    float4* v;      // velocity
+    float4* fo;     // force of the previous step
+    float4* facc;   // element-force accumulator (zeroed by the node pass)
+    float4* vp_a;   // viscoplastic P = Fp - I, entries 0..3
+    float4* vp_b;   // entries 4..7
+    float2* vp_c;   // entry 8, accumulated plastic strain
+    float2* fields; // von Mises, pressure per tetra (viscoplastic model)
+    unsigned* status;
+    long long* time;     // simulation time at the start of the current graph chunk
+    double* curve;       // 3 * max_rows: (t, indentation, force)
+    double* partials;    // one per node block, for the deterministic readout reduction
+    unsigned* counter;   // blocks finished in the readout reduction
+    double* force_out;   // scalar result of an on-demand readout
+};
+
+struct ContactDev {
+    int kind;
+    int pad;
+    double k, radius;
+    double p0, v, tmove;
+    // Optional per-step positions in device memory: meta = {t0, n}; n = 0 means "use the
+    // schedule". Kept in memory (not in the kernel parameters) so a captured graph stays
+    // valid when the host refills the table.
+    const double* table;
+    const long long* meta;
+};
+
+struct MaterialDev {
+    int model;
+    float mu1, mu2, kappa;  // Mooney-Rivlin / Neo-Hookean (and the viscoplastic elastic law)
+    float mu, kp;           // SVK / SVKK: mu and nu/(1-2nu)
+    float flow_exp, yield, flow_rate, hard_thr, hard_exp;
+};
+
+struct StepParams {
+    int n_contacts;
+    ContactDev c[MAX_CONTACTS];
+    int record_contact;        // -1: no force recording
+    long long record_every;    // 0: none
+    long long max_rows;
+    long long fields_every;    // tet fields written when (t+1) % fields_every == 0
+    float vv_a, vv_hb, vv_dm;  // v' = a v + hb (f + fo); dx = dm v' + f/2
+    int fix_a, fix_b;          // internal ids of the pinned nodes, -1 if none
+};
+
+// Kernel launchers (nfx_kernels.cu). All enqueue on `stream` and return cudaGetLastError().
+cudaError_t launch_tet_pass(const MeshDev& m, const StateDev& s, const MaterialDev& mat, const StepParams& p,
+                            int t_offset, cudaStream_t stream);
+enum NodeMode : int { NODE_UPDATE = 0, NODE_READOUT_ROW = 1, NODE_READOUT_VALUE = 2 };
+cudaError_t launch_node_pass(const MeshDev& m, const StateDev& s, const StepParams& p, int t_offset, int mode,
+                             int readout_contact, cudaStream_t stream);
+cudaError_t launch_advance_time(const StateDev& s, long long n, cudaStream_t stream);
+// Conversions between the user's layout (SoA doubles, user order) and the device state.
+cudaError_t launch_points_to_user(const MeshDev& m, const StateDev& s, const long long* node_user, double* out,
+                                  cudaStream_t stream);
+cudaError_t launch_points_from_user(const MeshDev& m, const StateDev& s, const long long* node_user,
+                                    const double* in, cudaStream_t stream);
+cudaError_t launch_vec_to_user(const MeshDev& m, const float4* a, const long long* node_user, double* out,
+                               cudaStream_t stream);
+cudaError_t launch_vec_from_user(const MeshDev& m, float4* a, const long long* node_user, const double* in,
+                                 cudaStream_t stream);
+cudaError_t launch_init_vp(const MeshDev& m, const StateDev& s, cudaStream_t stream);
+
+}  // namespace nfx

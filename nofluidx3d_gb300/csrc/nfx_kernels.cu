@@ -1,0 +1,398 @@
+// CUDA kernels of the noFluidX3D tetra-mesh step for sm_103a.
+//
+// One time step is two kernels:
+//   k_tet_pass  — one CTA per tile of tetrahedra: stage the tile's nodes (displacement hi/lo)
+//                 in shared memory, evaluate each tetra's material law in registers
+//                 (tetra.cl:14-182 or InteractionFiniteStrainViscoplastic.cl:1-220), sum the 12
+//                 nodal force components per tetra into shared-memory node slots, then flush one
+//                 float4 atomic per distinct node to the force accumulator. This replaces the
+//                 reference's 12 FP64 CAS loops per tetra (atomicAdd.cl:1-11).
+//   k_node_pass — one thread per node: accumulated element force + substrate/plane/sphere
+//                 contacts (Substrate.cl, Plane.cl, Sphere.cl), damped velocity Verlet
+//                 (VelocityVerlet.cl:1-36) with the displacement carried as float hi + lo,
+//                 zeroing of the accumulator, and on record steps the indenter-force readout of
+//                 Simulation.py:146-153 / :198-212 reduced with warp shuffles in a fixed order.
+// The kernel boundary is the step's only global barrier. Time t comes from device memory
+// (start of the captured chunk) plus the launch's offset, so a captured CUDA graph of G steps
+// can be replayed for any chunk.
+#include <cuda_runtime.h>
+
+#include "nfx_internal.h"
+#include "nfx_math.cuh"
+
+namespace nfx {
+
+__device__ __forceinline__ double contact_pos(const ContactDev& c, long long t) {
+    const long long n = c.meta[1];
+    if (n > 0) {
+        long long k = t - c.meta[0];
+        if (k < 0) k = 0;
+        if (k >= n) k = n - 1;
+        return c.table[k];
+    }
+    if (c.kind == CONTACT_SUBSTRATE) return c.p0;
+    const double tt = (double)t;
+    return tt <= c.tmove ? c.p0 - c.v * tt : c.p0 - c.v * c.tmove;
+}
+
+// ------------------------------------------------------------------------------------------
+// Element pass
+// ------------------------------------------------------------------------------------------
+template <int MODEL>
+__global__ void __launch_bounds__(TILE_TETS) k_tet_pass(MeshDev m, StateDev s, MaterialDev mat,
+                                                        long long fields_every, int t_offset) {
+    __shared__ float4 s_uh[TILE_NODES_MAX];
+    __shared__ float4 s_ul[TILE_NODES_MAX];
+    __shared__ float s_f[3 * TILE_NODES_MAX];
+
+    const int b = blockIdx.x;
+    const int j = threadIdx.x;
+    const int tb = m.tile_tet_begin[b];
+    const int ntt = m.tile_tet_begin[b + 1] - tb;
+    const int nb = m.tile_node_begin[b];
+    const int nn = m.tile_node_begin[b + 1] - nb;
+    const bool act = j < ntt;
+    const int t = tb + j;
+
+    // streaming per-tetra data first (read once per step: evict-first)
+    uchar4 lc = make_uchar4(0, 0, 0, 0);
+    float4 da = make_float4(0.f, 0.f, 0.f, 0.f), db = da;
+    float2 dc = make_float2(0.f, 0.f);
+    float4 pa = da, pb = da;
+    float2 pc = dc;
+    if (act) {
+        lc = __ldcs(m.lconn + t);
+        da = __ldcs(m.dmi_a + t);
+        db = __ldcs(m.dmi_b + t);
+        dc = __ldcs(m.dmi_c + t);
+        if (MODEL == MODEL_VP) {
+            pa = __ldcs(s.vp_a + t);
+            pb = __ldcs(s.vp_b + t);
+            pc = __ldcs(s.vp_c + t);
+        }
+    }
+    unsigned g = 0;
+    if (j < nn) {
+        g = m.tile_nodes[nb + j];
+        s_uh[j] = s.uh[g];
+        s_ul[j] = s.ul[g];
+        s_f[j] = 0.f;
+        s_f[TILE_NODES_MAX + j] = 0.f;
+        s_f[2 * TILE_NODES_MAX + j] = 0.f;
+    }
+    __syncthreads();
+
+    if (act) {
+        const int li[4] = {lc.x, lc.y, lc.z, lc.w};
+        const float4 u0h = s_uh[li[0]], u0l = s_ul[li[0]];
+        float d[3][3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const float4 h = s_uh[li[k + 1]], l = s_ul[li[k + 1]];
+            d[k][0] = (h.x - u0h.x) + (l.x - u0l.x);
+            d[k][1] = (h.y - u0h.y) + (l.y - u0l.y);
+            d[k][2] = (h.z - u0h.z) + (l.z - u0l.z);
+        }
+        const float Dmi[9] = {da.x, da.y, da.z, da.w, db.x, db.y, db.z, db.w, dc.x};
+        const float V0 = dc.y;
+        float f[4][3];
+        float jm1;
+        if (MODEL == MODEL_MR) {
+            jm1 = mr_element(d[0], d[1], d[2], Dmi, V0, mat.mu1, mat.mu2, mat.kappa, f);
+        } else if (MODEL == MODEL_SVK) {
+            jm1 = svk_element(d[0], d[1], d[2], Dmi, V0, mat.mu, mat.kp, f);
+        } else if (MODEL == MODEL_SVKK) {
+            jm1 = svkk_element(d[0], d[1], d[2], Dmi, V0, mat.mu, mat.kp, f);
+        } else {
+            VPParams par;
+            par.mu1 = mat.mu1;
+            par.mu2 = mat.mu2;
+            par.kappa = mat.kappa;
+            par.flow_exp = mat.flow_exp;
+            par.yield = mat.yield;
+            par.flow_rate = mat.flow_rate;
+            par.hard_thr = mat.hard_thr;
+            par.hard_exp = mat.hard_exp;
+            float P[9] = {pa.x, pa.y, pa.z, pa.w, pb.x, pb.y, pb.z, pb.w, pc.x};
+            float eps = pc.y;
+            float dP[9], rate, vm, pr;
+            vp_element(d[0], d[1], d[2], Dmi, V0, par, P, eps, dP, rate, f, vm, pr, jm1);
+#pragma unroll
+            for (int q = 0; q < 9; q++) P[q] += dP[q];
+            eps += rate;
+            __stcs(s.vp_a + t, make_float4(P[0], P[1], P[2], P[3]));
+            __stcs(s.vp_b + t, make_float4(P[4], P[5], P[6], P[7]));
+            __stcs(s.vp_c + t, make_float2(P[8], eps));
+            if (fields_every > 0) {
+                const long long tt = *s.time + t_offset;
+                if ((tt + 1) % fields_every == 0) __stcs(s.fields + t, make_float2(vm, pr));
+            }
+        }
+        if (!(jm1 > -1.0f)) atomicOr(s.status, STATUS_INVERTED);
+        const float chk = (f[0][0] + f[1][0]) + (f[2][0] + f[3][0]) + f[0][1] + f[1][2] + f[2][1] + f[3][2];
+        if (!isfinite(chk)) atomicOr(s.status, STATUS_NONFINITE);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            atomicAdd(&s_f[li[k]], f[k][0]);
+            atomicAdd(&s_f[TILE_NODES_MAX + li[k]], f[k][1]);
+            atomicAdd(&s_f[2 * TILE_NODES_MAX + li[k]], f[k][2]);
+        }
+    }
+    __syncthreads();
+    if (j < nn) {
+        const float4 acc = make_float4(s_f[j], s_f[TILE_NODES_MAX + j], s_f[2 * TILE_NODES_MAX + j], 0.f);
+        atomicAdd(s.facc + g, acc);
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Node pass
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Fixed-order grid reduction of one double per thread. The last block to finish sums the
+// per-block partials in index order, so the result is the same on every run.
+__device__ void grid_sum_finish(const StateDev& s, double val, bool to_scalar, long long row, long long t,
+                                double indentation) {
+    __shared__ double s_w[NODE_BLOCK / 32];
+    __shared__ int s_last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    val = warp_sum_d(val);
+    if (lane == 0) s_w[warp] = val;
+    __syncthreads();
+    if (warp == 0) {
+        double x = lane < NODE_BLOCK / 32 ? s_w[lane] : 0.0;
+        x = warp_sum_d(x);
+        if (lane == 0) {
+            s.partials[blockIdx.x] = x;
+            __threadfence();
+            const unsigned prev = atomicAdd(s.counter, 1u);
+            s_last = prev == gridDim.x - 1;
+        }
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    double acc = 0.0;
+    const volatile double* part = s.partials;
+    for (int k = threadIdx.x; k < (int)gridDim.x; k += NODE_BLOCK) acc += part[k];
+    acc = warp_sum_d(acc);
+    if (lane == 0) s_w[warp] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tot = 0.0;
+        for (int w = 0; w < NODE_BLOCK / 32; w++) tot += s_w[w];
+        if (to_scalar) {
+            *s.force_out = tot;
+        } else {
+            s.curve[3 * row] = (double)t;
+            s.curve[3 * row + 1] = indentation;
+            s.curve[3 * row + 2] = tot;
+        }
+        *s.counter = 0u;
+    }
+}
+
+// Contact force on one node in double precision (the reference's FP64 formulas). Returns the
+// y component for the readout; adds the force to f.
+__device__ __forceinline__ double contact_force(const ContactDev& c, double w, const float4& xh, const float4& xl,
+                                                const float4& uh, const float4& ul, float4& f) {
+    // coarse test in float: nodes farther than 1e-3 from contact cannot touch
+    const float yf = xh.y + uh.y;
+    if (c.kind == CONTACT_SUBSTRATE) {
+        if ((float)w - yf < -1e-3f) return 0.0;
+        const double y = ((double)xh.y + (double)xl.y) + ((double)uh.y + (double)ul.y);
+        const double dis = fmax(w - y, 0.0);
+        const double fy = c.k * dis;
+        f.y += (float)fy;
+        return fy;
+    }
+    if (c.kind == CONTACT_PLANE) {
+        if (yf - (float)w < -1e-3f) return 0.0;
+        const double y = ((double)xh.y + (double)xl.y) + ((double)uh.y + (double)ul.y);
+        const double dis = fmax(y - w, 0.0);
+        const double fy = -c.k * dis;
+        f.y += (float)fy;
+        return fy;
+    }
+    // sphere centred at (0, w, 0)
+    const float rxf = xh.x + uh.x, ryf = yf - (float)w, rzf = xh.z + uh.z;
+    const float rr = (float)c.radius + 1e-3f;
+    if (rxf * rxf + ryf * ryf + rzf * rzf > rr * rr) return 0.0;
+    const double rx = ((double)xh.x + (double)xl.x) + ((double)uh.x + (double)ul.x);
+    const double ry = (((double)xh.y + (double)xl.y) + ((double)uh.y + (double)ul.y)) - w;
+    const double rz = ((double)xh.z + (double)xl.z) + ((double)uh.z + (double)ul.z);
+    const double len = sqrt(rx * rx + ry * ry + rz * rz);
+    const double dis = fmax(c.radius - len, 0.0);
+    if (dis == 0.0) return 0.0;
+    const double kd = c.k * dis;
+    const double fx = kd * (rx / len), fy = kd * (ry / len), fz = kd * (rz / len);
+    f.x += (float)fx;
+    f.y += (float)fy;
+    f.z += (float)fz;
+    return fy;
+}
+
+__global__ void __launch_bounds__(NODE_BLOCK) k_node_pass(MeshDev m, StateDev s, StepParams p, int t_offset,
+                                                          int mode, int readout_contact) {
+    const int i = blockIdx.x * NODE_BLOCK + threadIdx.x;
+    const long long t = *s.time + t_offset;
+    int rc;
+    bool rec;
+    long long row = 0;
+    if (mode == NODE_READOUT_VALUE) {
+        rc = readout_contact;
+        rec = true;
+    } else {
+        rc = p.record_contact;
+        rec = rc >= 0 && p.record_every > 0 && (t % p.record_every) == 0;
+        if (rec) {
+            row = t / p.record_every;
+            if (row >= p.max_rows) {
+                if (i == 0) atomicOr(s.status, STATUS_CURVE_FULL);
+                rec = false;
+            }
+        }
+    }
+    double ro = 0.0;
+    if (i < m.np) {
+        float4 f = s.facc[i];
+        const float4 xh = m.Xh[i], xl = m.Xl[i];
+        float4 uh = s.uh[i], ul = s.ul[i];
+        for (int c = 0; c < p.n_contacts; c++) {
+            const double w = contact_pos(p.c[c], t);
+            const double fy = contact_force(p.c[c], w, xh, xl, uh, ul, f);
+            if (c == rc) ro = -fy;
+        }
+        if (mode == NODE_UPDATE) {
+            float4 v = s.v[i];
+            const float4 fo = s.fo[i];
+            v.x = p.vv_a * v.x + p.vv_hb * (f.x + fo.x);
+            v.y = p.vv_a * v.y + p.vv_hb * (f.y + fo.y);
+            v.z = p.vv_a * v.z + p.vv_hb * (f.z + fo.z);
+            df_add(uh.x, ul.x, p.vv_dm * v.x + 0.5f * f.x);
+            df_add(uh.y, ul.y, p.vv_dm * v.y + 0.5f * f.y);
+            df_add(uh.z, ul.z, p.vv_dm * v.z + 0.5f * f.z);
+            if (i == p.fix_a || i == p.fix_b) {  // VelocityVerlet.cl:17-22: x = z = 0
+                uh.x = -xh.x;
+                ul.x = -xl.x;
+                uh.z = -xh.z;
+                ul.z = -xl.z;
+            }
+            if (!isfinite(uh.x + uh.y + uh.z + v.x + v.y + v.z)) atomicOr(s.status, STATUS_NONFINITE);
+            s.uh[i] = uh;
+            s.ul[i] = ul;
+            s.v[i] = v;
+            s.fo[i] = make_float4(f.x, f.y, f.z, 0.f);
+            s.facc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    }
+    if (rec) {
+        double ind = 0.0;
+        if (rc >= 0 && rc < p.n_contacts) ind = contact_pos(p.c[rc], 0) - contact_pos(p.c[rc], t);
+        grid_sum_finish(s, ro, mode == NODE_READOUT_VALUE, row, t, ind);
+    }
+}
+
+__global__ void k_advance_time(long long* time, long long n) { *time += n; }
+
+// ------------------------------------------------------------------------------------------
+// Layout conversions (user order, SoA doubles) <-> device state
+// ------------------------------------------------------------------------------------------
+__global__ void k_points_to_user(MeshDev m, StateDev s, const long long* node_user, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.np) return;
+    const long long u = node_user[i];
+    const float4 xh = m.Xh[i], xl = m.Xl[i], uh = s.uh[i], ul = s.ul[i];
+    out[u] = ((double)xh.x + (double)xl.x) + ((double)uh.x + (double)ul.x);
+    out[m.np + u] = ((double)xh.y + (double)xl.y) + ((double)uh.y + (double)ul.y);
+    out[2 * (long long)m.np + u] = ((double)xh.z + (double)xl.z) + ((double)uh.z + (double)ul.z);
+}
+
+__global__ void k_points_from_user(MeshDev m, StateDev s, const long long* node_user, const double* in) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.np) return;
+    const long long u = node_user[i];
+    const float4 xh = m.Xh[i], xl = m.Xl[i];
+    const double dx = (in[u] - (double)xh.x) - (double)xl.x;
+    const double dy = (in[m.np + u] - (double)xh.y) - (double)xl.y;
+    const double dz = (in[2 * (long long)m.np + u] - (double)xh.z) - (double)xl.z;
+    const float hx = (float)dx, hy = (float)dy, hz = (float)dz;
+    s.uh[i] = make_float4(hx, hy, hz, 0.f);
+    s.ul[i] = make_float4((float)(dx - hx), (float)(dy - hy), (float)(dz - hz), 0.f);
+}
+
+__global__ void k_vec_to_user(int np, const float4* a, const long long* node_user, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    const long long u = node_user[i];
+    const float4 q = a[i];
+    out[u] = q.x;
+    out[np + u] = q.y;
+    out[2 * (long long)np + u] = q.z;
+}
+
+__global__ void k_vec_from_user(int np, float4* a, const long long* node_user, const double* in) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    const long long u = node_user[i];
+    a[i] = make_float4((float)in[u], (float)in[np + u], (float)in[2 * (long long)np + u], 0.f);
+}
+
+// ------------------------------------------------------------------------------------------
+// Launchers
+// ------------------------------------------------------------------------------------------
+cudaError_t launch_tet_pass(const MeshDev& m, const StateDev& s, const MaterialDev& mat, const StepParams& p,
+                            int t_offset, cudaStream_t st) {
+    const dim3 grid((unsigned)m.ntiles), block(TILE_TETS);
+    switch (mat.model) {
+        case MODEL_MR: k_tet_pass<MODEL_MR><<<grid, block, 0, st>>>(m, s, mat, p.fields_every, t_offset); break;
+        case MODEL_SVK: k_tet_pass<MODEL_SVK><<<grid, block, 0, st>>>(m, s, mat, p.fields_every, t_offset); break;
+        case MODEL_SVKK: k_tet_pass<MODEL_SVKK><<<grid, block, 0, st>>>(m, s, mat, p.fields_every, t_offset); break;
+        case MODEL_VP: k_tet_pass<MODEL_VP><<<grid, block, 0, st>>>(m, s, mat, p.fields_every, t_offset); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_node_pass(const MeshDev& m, const StateDev& s, const StepParams& p, int t_offset, int mode,
+                             int readout_contact, cudaStream_t st) {
+    const unsigned blocks = (unsigned)((m.np + NODE_BLOCK - 1) / NODE_BLOCK);
+    k_node_pass<<<blocks, NODE_BLOCK, 0, st>>>(m, s, p, t_offset, mode, readout_contact);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_advance_time(const StateDev& s, long long n, cudaStream_t st) {
+    k_advance_time<<<1, 1, 0, st>>>(s.time, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_points_to_user(const MeshDev& m, const StateDev& s, const long long* node_user, double* out,
+                                  cudaStream_t st) {
+    k_points_to_user<<<(m.np + 255) / 256, 256, 0, st>>>(m, s, node_user, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_points_from_user(const MeshDev& m, const StateDev& s, const long long* node_user,
+                                    const double* in, cudaStream_t st) {
+    k_points_from_user<<<(m.np + 255) / 256, 256, 0, st>>>(m, s, node_user, in);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_vec_to_user(const MeshDev& m, const float4* a, const long long* node_user, double* out,
+                               cudaStream_t st) {
+    k_vec_to_user<<<(m.np + 255) / 256, 256, 0, st>>>(m.np, a, node_user, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_vec_from_user(const MeshDev& m, float4* a, const long long* node_user, const double* in,
+                                 cudaStream_t st) {
+    k_vec_from_user<<<(m.np + 255) / 256, 256, 0, st>>>(m.np, a, node_user, in);
+    return cudaGetLastError();
+}
+
+}  // namespace nfx

@@ -1,0 +1,194 @@
+// Host-side mesh plan: locality reordering, tiles and per-tetra reference quantities.
+//
+// The reference keeps the user's node and tetra order and recomputes the inverse reference
+// edge matrix every step (tetra.cl:47-53). Here, once at set-up:
+//  * nodes are sorted along a Morton (Z-order) curve of their reference positions, and tetrahedra
+//    along the Morton curve of their centroids, so a run of consecutive tetrahedra touches a
+//    compact set of nodes;
+//  * consecutive tetrahedra are grouped into tiles of at most TILE_TETS elements and
+//    TILE_NODES_MAX distinct nodes, each tetra's corners stored as 8-bit indices into its
+//    tile's node list;
+//  * Dm^-1 (inverse of the reference edge matrix [X1-X0, X2-X0, X3-X0]) and the signed
+//    reference volume V0 = det(Dm)/6 (TetraCell.py:33-41) are computed in double and stored
+//    as float;
+//  * reference positions are split into float hi + lo parts.
+// Corner order within a tetra is the user's, so node 0 of each tetra stays the base node of
+// the reference's elastic kernel (tetra.cl:31-35).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+#include "nfx_internal.h"
+
+namespace nfx {
+
+namespace {
+
+inline uint64_t spread3(uint64_t x) {
+    x &= 0x1fffff;  // 21 bits
+    x = (x | (x << 32)) & 0x1f00000000ffffULL;
+    x = (x | (x << 16)) & 0x1f0000ff0000ffULL;
+    x = (x | (x << 8)) & 0x100f00f00f00f00fULL;
+    x = (x | (x << 4)) & 0x10c30c30c30c30c3ULL;
+    x = (x | (x << 2)) & 0x1249249249249249ULL;
+    return x;
+}
+
+inline uint64_t morton3(uint64_t x, uint64_t y, uint64_t z) { return spread3(x) | (spread3(y) << 1) | (spread3(z) << 2); }
+
+struct Quant {
+    double lo[3];
+    double inv_h;
+    uint64_t q(double v, int d) const {
+        double s = (v - lo[d]) * inv_h;
+        if (!(s > 0)) s = 0;
+        if (s > 2097151.0) s = 2097151.0;
+        return (uint64_t)s;
+    }
+};
+
+}  // namespace
+
+bool build_mesh_plan(int64_t np, int64_t nt, const double* P, const uint32_t* T, MeshPlan& plan, std::string& err) {
+    if (np <= 0 || nt <= 0) {
+        err = "mesh needs at least one node and one tetra";
+        return false;
+    }
+    if (np > (int64_t)0x7fffffff || nt > (int64_t)0x7fffffff) {
+        err = "mesh too large (more than 2^31-1 nodes or tetrahedra)";
+        return false;
+    }
+    for (int64_t t = 0; t < 4 * nt; t++) {
+        if ((int64_t)T[t] >= np) {
+            err = "tetra corner index out of range";
+            return false;
+        }
+    }
+    for (int64_t i = 0; i < 3 * np; i++) {
+        if (!std::isfinite(P[i])) {
+            err = "non-finite node position";
+            return false;
+        }
+    }
+    plan = MeshPlan();
+    plan.np = np;
+    plan.nt = nt;
+
+    // quantisation: cell size ~ mean node spacing
+    Quant Q;
+    double hi[3];
+    for (int d = 0; d < 3; d++) {
+        Q.lo[d] = P[d * np];
+        hi[d] = P[d * np];
+        for (int64_t i = 1; i < np; i++) {
+            Q.lo[d] = std::min(Q.lo[d], P[d * np + i]);
+            hi[d] = std::max(hi[d], P[d * np + i]);
+        }
+    }
+    double vol = 1.0;
+    for (int d = 0; d < 3; d++) vol *= std::max(hi[d] - Q.lo[d], 1e-12);
+    double h = std::cbrt(vol / (double)np);
+    if (!(h > 0)) h = 1.0;
+    Q.inv_h = 1.0 / h;
+
+    // nodes
+    std::vector<uint64_t> nkey(np);
+    for (int64_t i = 0; i < np; i++)
+        nkey[i] = morton3(Q.q(P[i], 0), Q.q(P[np + i], 1), Q.q(P[2 * np + i], 2));
+    plan.node_user.resize(np);
+    std::iota(plan.node_user.begin(), plan.node_user.end(), 0);
+    std::stable_sort(plan.node_user.begin(), plan.node_user.end(),
+                     [&](int64_t a, int64_t b) { return nkey[a] < nkey[b]; });
+    plan.node_int.resize(np);
+    for (int64_t i = 0; i < np; i++) plan.node_int[plan.node_user[i]] = i;
+
+    // tetrahedra, by centroid
+    std::vector<uint64_t> tkey(nt);
+    for (int64_t t = 0; t < nt; t++) {
+        double c[3] = {0, 0, 0};
+        for (int k = 0; k < 4; k++) {
+            const int64_t n = T[k * nt + t];
+            for (int d = 0; d < 3; d++) c[d] += 0.25 * P[d * np + n];
+        }
+        tkey[t] = morton3(Q.q(c[0], 0), Q.q(c[1], 1), Q.q(c[2], 2));
+    }
+    plan.tet_user.resize(nt);
+    std::iota(plan.tet_user.begin(), plan.tet_user.end(), 0);
+    std::stable_sort(plan.tet_user.begin(), plan.tet_user.end(),
+                     [&](int64_t a, int64_t b) { return tkey[a] < tkey[b]; });
+
+    // tiles
+    plan.lconn.resize(4 * (size_t)nt);
+    plan.tile_tet_begin.push_back(0);
+    plan.tile_node_begin.push_back(0);
+    std::vector<uint32_t> ids;
+    ids.reserve(4 * TILE_TETS);
+    int64_t t0 = 0;
+    while (t0 < nt) {
+        int64_t cnt = std::min<int64_t>(TILE_TETS, nt - t0);
+        for (;;) {
+            ids.clear();
+            for (int64_t j = 0; j < cnt; j++) {
+                const int64_t ut = plan.tet_user[t0 + j];
+                for (int k = 0; k < 4; k++) ids.push_back((uint32_t)plan.node_int[T[k * nt + ut]]);
+            }
+            std::sort(ids.begin(), ids.end());
+            ids.erase(std::unique(ids.begin(), ids.end()), ids.end());
+            if ((int64_t)ids.size() <= TILE_NODES_MAX || cnt == 1) break;
+            cnt = std::max<int64_t>(1, cnt - 16);
+        }
+        for (int64_t j = 0; j < cnt; j++) {
+            const int64_t ut = plan.tet_user[t0 + j];
+            for (int k = 0; k < 4; k++) {
+                const uint32_t g = (uint32_t)plan.node_int[T[k * nt + ut]];
+                const size_t loc = std::lower_bound(ids.begin(), ids.end(), g) - ids.begin();
+                plan.lconn[4 * (t0 + j) + k] = (uint8_t)loc;
+            }
+        }
+        plan.tile_nodes.insert(plan.tile_nodes.end(), ids.begin(), ids.end());
+        t0 += cnt;
+        plan.tile_tet_begin.push_back((int32_t)t0);
+        plan.tile_node_begin.push_back((int32_t)plan.tile_nodes.size());
+    }
+    plan.ntiles = (int64_t)plan.tile_tet_begin.size() - 1;
+
+    // per-tetra Dm^-1 and V0 (internal order)
+    plan.dmi.assign(12 * (size_t)nt, 0.0f);
+    for (int64_t it = 0; it < nt; it++) {
+        const int64_t ut = plan.tet_user[it];
+        const int64_t n0 = T[ut];
+        double M[9];  // columns X_k - X_0
+        for (int k = 0; k < 3; k++) {
+            const int64_t nk = T[(k + 1) * nt + ut];
+            for (int d = 0; d < 3; d++) M[3 * d + k] = P[d * np + nk] - P[d * np + n0];
+        }
+        const double A[9] = {M[4] * M[8] - M[5] * M[7], M[2] * M[7] - M[1] * M[8], M[1] * M[5] - M[2] * M[4],
+                             M[5] * M[6] - M[3] * M[8], M[0] * M[8] - M[2] * M[6], M[2] * M[3] - M[0] * M[5],
+                             M[3] * M[7] - M[4] * M[6], M[1] * M[6] - M[0] * M[7], M[0] * M[4] - M[1] * M[3]};
+        const double det = M[0] * A[0] + M[1] * A[3] + M[2] * A[6];
+        if (det == 0.0 || !std::isfinite(det)) {
+            err = "degenerate tetra (zero reference volume) at index " + std::to_string(ut);
+            return false;
+        }
+        float* o = &plan.dmi[12 * it];
+        for (int k = 0; k < 9; k++) o[k] = (float)(A[k] / det);
+        o[9] = (float)(det / 6.0);
+    }
+
+    // reference positions, hi/lo, internal order
+    plan.Xh.assign(4 * (size_t)np, 0.0f);
+    plan.Xl.assign(4 * (size_t)np, 0.0f);
+    for (int64_t i = 0; i < np; i++) {
+        const int64_t u = plan.node_user[i];
+        for (int d = 0; d < 3; d++) {
+            const double x = P[d * np + u];
+            const float h32 = (float)x;
+            plan.Xh[4 * i + d] = h32;
+            plan.Xl[4 * i + d] = (float)(x - (double)h32);
+        }
+    }
+    return true;
+}
+
+}  // namespace nfx

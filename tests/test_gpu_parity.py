@@ -1,0 +1,161 @@
+"""Parity of the CUDA step (through the C ABI) with the reference: golden vectors from the
+reference's own kernels and the FP64 oracle run live. Tolerances are the spec bars:
+node trajectories within 1e-5 relative, force-depth curves within 1e-4 relative (L2 over the
+recorded rows); the FP32 kernels carry the displacement as hi+lo floats."""
+
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from nofluidx3d_gb300.core import CellSim
+from nofluidx3d_gb300.workloads import Workload, plain_small
+from tests.golden.cases import CASES
+from tests.helpers import oracle_problem, rel_curve, rel_disp, rel_traj
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+TRAJ_TOL = 1e-5
+CURVE_TOL = 1e-4
+
+
+def gpu_case(case, steps=None):
+    w = case.workload
+    sim = CellSim(0)
+    m = w.configure(sim)
+    if case.model is not None:
+        model, E, nu, mr = w.tetra_params()
+        sim.set_tetra(case.model, E, nu, mr)
+    if case.fix_top_bottom:
+        sim.set_integrator(w.xi, True)
+    n = case.steps if steps is None else steps
+    sim.step(n)
+    sim.record_now()
+    return sim, m
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_gpu_matches_golden(name):
+    case = CASES[name]
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    sim, m = gpu_case(case)
+    x = sim.points()
+    c = sim.curve()
+    assert sim.status() == 0
+    assert rel_traj(g["points"], x) < TRAJ_TOL
+    assert rel_disp(g["points"], x, m.points) < 1e-3
+    assert rel_curve(g["curve"], c) < CURVE_TOL, (g["curve"], c)
+    if "Fp" in g:
+        Fp = sim.plastic_tensor_soa()
+        np.testing.assert_allclose(Fp, g["Fp"], atol=1e-5)
+    if case.fix_top_bottom:
+        ids = [3, 4]
+        assert np.all(x[ids, 0] == 0.0) and np.all(x[ids, 2] == 0.0)
+    sim.close()
+
+
+def test_gpu_plain_small_10k_steps_vs_fp64_oracle():
+    """The plain small workload (R=8 NH, 13,056 tetra) for 10^4 steps against the FP64 oracle."""
+    w = plain_small()
+    n = 10000
+    mesh = w.mesh()
+    st = O.State(oracle_problem(w, mesh), "f64")
+    cref = st.run(n, w.record_every)
+    sim = CellSim(0)
+    w.configure(sim, mesh)
+    sim.step(n)
+    sim.record_now()
+    x = sim.points()
+    c = sim.curve()
+    assert sim.status() == 0
+    e_traj = rel_traj(st.positions(), x)
+    e_curve = rel_curve(cref, c)
+    print(f"plain-small 1e4 steps: trajectory rel {e_traj:.3e}, curve rel {e_curve:.3e}")
+    assert e_traj < TRAJ_TOL
+    assert e_curve < CURVE_TOL
+    sim.close()
+
+
+def test_gpu_single_tetra_force():
+    """One step from a deformed single tetra: the stored previous force equals the oracle's
+    element force (tetra.cl) for NH, MR, SVK and SVKK."""
+    X = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], float)
+    T = np.array([[0, 1, 2, 3]])
+    rng = np.random.default_rng(3)
+    x = X + rng.uniform(-0.05, 0.05, X.shape)
+    for model, mr in [(O.MODEL_MR, 1.0), (O.MODEL_MR, 0.7), (O.MODEL_SVK, 1.0), (O.MODEL_SVKK, 1.0)]:
+        P = O.Problem(X, T, model=model, E=3e-3, nu=0.45, mr=mr, xi=0.0)
+        st = O.State(P, "f64")
+        st.points[:] = x.T.reshape(-1)
+        st.run(1)
+        sim = CellSim(0)
+        sim.set_mesh(X, T)
+        sim.set_tetra(model, 3e-3, 0.45, mr)
+        sim.set_integrator(0.0)
+        sim.set_points(x)
+        sim.step(1)
+        f_gpu = sim.force_old()
+        f_ref = st.fold.reshape(3, -1).T
+        np.testing.assert_allclose(f_gpu, f_ref, rtol=2e-4, atol=1e-9 * np.abs(f_ref).max())
+        np.testing.assert_allclose(sim.points(), st.positions(), rtol=0, atol=1e-7)
+        sim.close()
+
+
+def test_gpu_graph_chunks_match_single_steps():
+    w = CASES["nh_plane_R3"].workload
+    a, b = CellSim(0), CellSim(0)
+    w.configure(a)
+    w.configure(b)
+    a.step(250)  # two captured 100-step graphs + 50 single steps
+    for _ in range(250):
+        b.step(1)
+    np.testing.assert_allclose(a.points(), b.points(), rtol=0, atol=1e-6)
+    a.record_now()
+    b.record_now()
+    np.testing.assert_allclose(a.curve(), b.curve(), rtol=1e-4, atol=1e-12)
+    a.close()
+    b.close()
+
+
+def test_gpu_indenter_force_equals_recorded_row():
+    w = CASES["nh_plane_R3"].workload
+    sim = CellSim(0)
+    w.configure(sim)
+    sim.step(100)
+    f = sim.indenter_force(1)
+    sim.record_now()
+    c = sim.curve()
+    assert c.shape[0] == 3 and c[-1, 0] == 100
+    assert f == c[-1, 2]
+    sim.close()
+
+
+def test_gpu_contact_table_equals_schedule():
+    """Per-step positions from a host table (arbitrary wallFunc) give the same run as the
+    on-device linear schedule."""
+    w = CASES["nh_plane_R3"].workload
+    a, b = CellSim(0), CellSim(0)
+    w.configure(a)
+    w.configure(b)
+    c = w.contacts()[1]
+    t = np.arange(0, 300, dtype=np.float64)
+    b.set_contact_table(1, 0, c["p0"] - c["v"] * t)
+    a.step(300)
+    b.step(300)
+    np.testing.assert_allclose(a.points(), b.points(), rtol=0, atol=1e-6)
+    a.close()
+    b.close()
+
+
+def test_gpu_nonfinite_input_raises_status():
+    w = CASES["nh_plane_R3"].workload
+    sim = CellSim(0)
+    m = w.configure(sim)
+    x = m.points.copy()
+    x[10, 1] = np.nan
+    sim.set_points(x)
+    sim.step(2)
+    assert sim.status() & 1
+    sim.close()

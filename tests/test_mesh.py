@@ -1,0 +1,65 @@
+"""Synthetic Kuhn-sphere meshes and workload parameter mappings. CPU only."""
+
+import numpy as np
+import pytest
+
+from nofluidx3d_gb300.mesh import edge_vectors, kuhn_sphere, mesh_counts, signed_volumes
+from nofluidx3d_gb300.workloads import nh_to_reference, plain_large, plain_small
+
+
+@pytest.mark.parametrize("R,expect", [(6, (912, 5472, 1285)), (8, (2176, 13056, 2849)),
+                                      (16, (17256, 103536, 19789))])
+def test_counts(R, expect):
+    assert mesh_counts(R) == expect
+    m = kuhn_sphere(R)
+    assert (m.num_tetra, m.num_points) == expect[1:]
+
+
+def test_conventions_and_orientation():
+    m = kuhn_sphere(8, 0.02, 0)
+    p = m.points
+    np.testing.assert_array_equal(p[0], [0, 0, 0])
+    np.testing.assert_array_equal(p[1], [8, 0, 0])
+    np.testing.assert_array_equal(p[3], [0, 8, 0])
+    np.testing.assert_array_equal(p[4], [0, -8, 0])
+    v = signed_volumes(p, m.tets)
+    assert v.min() > 0
+    assert abs(v.sum() - 2176.0) < 1e-9  # jitter of interior nodes preserves the total volume
+    # conforming: every interior face is shared by exactly two tets
+    faces = np.sort(np.concatenate([m.tets[:, [0, 1, 2]], m.tets[:, [0, 1, 3]], m.tets[:, [0, 2, 3]],
+                                    m.tets[:, [1, 2, 3]]]), axis=1)
+    _, cnt = np.unique(faces, axis=0, return_counts=True)
+    assert set(np.unique(cnt)) <= {1, 2}
+
+
+def test_jitter_is_seeded_and_bounded():
+    a = kuhn_sphere(6, 0.02, 5)
+    b = kuhn_sphere(6, 0.02, 5)
+    c = kuhn_sphere(6, 0.02, 6)
+    g = kuhn_sphere(6, 0.0)
+    np.testing.assert_array_equal(a.points, b.points)
+    assert not np.array_equal(a.points, c.points)
+    d = np.abs(a.points - g.points)
+    assert d.max() <= 0.02 and d.max() > 0.015
+
+
+def test_edge_vector_bases():
+    m = kuhn_sphere(4)
+    e0 = edge_vectors(m.points, m.tets, 0)
+    e3 = edge_vectors(m.points, m.tets, 3)
+    np.testing.assert_allclose(e0[:, 0:3], m.points[m.tets[:, 1]] - m.points[m.tets[:, 0]])
+    np.testing.assert_allclose(e3[:, 0:3], m.points[m.tets[:, 0]] - m.points[m.tets[:, 3]])
+
+
+def test_nh_mapping_recovers_moduli():
+    E, nu = nh_to_reference(1e-3, 1e-2)
+    assert abs(E / (2 * (1 + nu)) - 1e-3) < 1e-15
+    assert abs(E / (3 * (1 - 2 * nu)) - 1e-2) < 1e-15
+
+
+def test_workload_definitions():
+    s, l = plain_small(), plain_large()
+    assert s.radius == 8 and s.steps == 20000 and s.record_every == 100
+    assert l.radius == 64 and l.material == "mr_vp" and l.indenter == "sphere" and l.sphere_radius == 16
+    par = l.vp_params()
+    assert par[0] == 1e-3 and par[1] == 2e-4 and par[5] == pytest.approx(4e-3)
