@@ -110,7 +110,9 @@ int nfx_set_integrator(nfx_sim* sim, double xi, int fix_top_bottom);
 /* Records the indenter force of contact `contact` every `every` steps into a device buffer of
  * max_rows rows (t, indentation, force) — the recordedQuantities currentTime / indentationSI /
  * forceSI of Simulation.py:94-100, :142-157, :194-216 in lattice units. Row r is time r*every.
- * Per-tetra fields are refreshed on the same interval. contact = -1 disables recording. */
+ * Per-tetra fields (von Mises, pressure) are written by the step whose end time is a multiple of
+ * `every`, as the reference's buffers hold the last step's values at each output
+ * (util/IO.py:30-35). contact = -1 records no force rows but keeps the field interval. */
 int nfx_set_record(nfx_sim* sim, int contact, int64_t every, int64_t max_rows);
 
 /* Enqueues nsteps time steps (Simulation.timeStep, Simulation.py:232-237, nsteps times). */
@@ -170,6 +172,7 @@ int nfx_profile_steps(nfx_sim* sim, int64_t nsteps, float* tet_ms, float* node_m
 
 /* Number of mesh tiles and distinct-node entries (diagnostics for the tile layout). */
 int nfx_mesh_info(nfx_sim* sim, int64_t* ntiles, int64_t* tile_nodes);
+
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,219 @@
+"""Simulation driver, mirroring nofluidx3d/Simulation.py:34-290.
+
+Same JSON configuration, unit conversion, interaction set-up and output loop as the reference;
+the difference is underneath: the shared buffers live in one nfx_sim handle (a CellSim) on the
+GPU, plugins hand it their parameters, and timeStep()/run() advance the whole fused step through
+the C ABI. Output frames are legacy-VTK files; non-finite positions raise FloatingPointError
+instead of exit().
+
+`con` is a path to the reference's JSON config or an already-parsed dict with the same keys.
+"""
+
+from __future__ import annotations
+
+import json
+import os
+import time
+
+import numpy as np
+
+from .core import CellSim
+from .interactions import FiniteStrainViscoplastic, Plane, Sphere, Substrate, Tetra, VelocityVerlet
+from .TetraCell import TetraCell
+from .util.Bridge import Bridge
+from .util.IO import writeVTK
+
+
+def _linear_schedule(p0: float, v: float, tmove: float):
+    """The reference's wallFunc/sphereFunc shape (Simulation.py:117-132, :173-183), tagged so the
+    position runs on the device."""
+
+    def f(time):
+        if time <= tmove:
+            return p0 - v * time
+        return p0 - v * tmove
+
+    f.nfx_schedule = (p0, v, tmove)
+    return f
+
+
+class Simulation:
+    def __init__(self, con, verbose: bool = True):
+        if isinstance(con, dict):
+            self.parameters = con
+        else:
+            with open(con) as configfile:
+                self.parameters = json.load(configfile)
+        self.verbose = verbose
+        device = int(self.parameters.get("gpu", 0))
+
+        # conversion constants (Simulation.py:41-53)
+        rho = 1.0
+        self.rho0 = self.parameters["RhoSI"] / rho
+        self.L0 = self.parameters["CELL"]["RadiusSI"] / self.parameters["CELL"]["RadiusSIM"]
+        E = 1e-2
+        self.p0 = self.parameters["CELL"]["YoungsModulusSI"] / E
+        self.V0 = np.sqrt(self.p0 / self.rho0)
+        self.T0 = self.L0 / self.V0
+        self._print(f"V0={self.V0}")
+        self._print(f"T0={self.T0}")
+
+        self.Nsteps = int(round(self.parameters["SimulationTimeSI"] / self.T0))
+        self.VTKInterval = int(round(self.Nsteps / self.parameters["VTKFramesTotal"]))
+        self.vtkfilespath = self.parameters["OutputDir"] + "vtkfiles/frame"
+        os.makedirs(self.parameters["OutputDir"] + "vtkfiles", exist_ok=True)
+
+        self.cell = TetraCell(self.parameters["CELL"]["InitVTK"], radius=self.parameters["CELL"]["RadiusSIM"],
+                              recenter=True)
+        self.numPoints = self.cell.points[:, 0].size
+        self.numTetra = self.cell.tetras[:, 0].size
+        self._print(f"Particle mesh consists of {self.numPoints} vertices and {self.numTetra} tetrahedrons")
+        self.interactions = []
+        self.time = 0
+
+        # the device state (shared buffers of Simulation.py:82-90)
+        self.handle = CellSim(device)
+        self.handle.set_mesh(self.cell.points, self.cell.tetras)
+        # per-tetra fields are refreshed by the last step of every output interval
+        self.handle.set_record(-1, max(self.VTKInterval, 1), 0)
+        self.points = Bridge(self.cell.points.reshape(3 * self.numPoints, order="F"), np.float64,
+                             read=lambda a: self.handle.points_soa(out=a), write=lambda a: self.handle.set_points(a))
+        self.tetras = Bridge(self.cell.tetras.reshape(4 * self.numTetra, order="F"), np.uint32)
+        # VelocityVerlet.cl zeroes the force buffer at the end of every step (:33-35)
+        self.force = Bridge(np.zeros(self.numPoints * 3), np.float64, read=lambda a: a.fill(0.0))
+        self.vonMises = Bridge(np.zeros(self.numTetra), np.float64,
+                               read=lambda a: a.__setitem__(slice(None), self.handle.tet_field(0)))
+        self.pressure = Bridge(np.zeros(self.numTetra), np.float64,
+                               read=lambda a: a.__setitem__(slice(None), self.handle.tet_field(1)))
+
+        self.recordedQuantities = []
+
+        def currentTime():
+            return self.time
+
+        self.recordedQuantities.append(currentTime)
+
+    def _print(self, *a, **k):
+        if self.verbose:
+            print(*a, **k)
+
+    def register(self, interaction):
+        interaction.register(self)
+        self.interactions.append(interaction)
+
+    def setInteractionSubstrate(self):
+        wallPosition = -(self.parameters["CELL"]["RadiusSIM"] + self.parameters["InitialDistance"])
+        forceConst = 0.1
+        self.register(Substrate(wallPosition, forceConst))
+
+    def _move_params(self):
+        v = self.parameters["VelocitySI"] / self.V0
+        tmove = self.parameters["MoveTimeSI"] / self.T0
+        return v, tmove
+
+    def setInteractionPlane(self, record=True):
+        p0 = self.parameters["CELL"]["RadiusSIM"] + self.parameters["InitialDistance"]
+        v, tmove = self._move_params()
+        wallFunc = _linear_schedule(p0, v, tmove)
+        forceConst = 0.1
+        plane = Plane(wallFunc, forceConst)
+        self.register(plane)
+
+        def indentationSI():
+            return (wallFunc(0) - wallFunc(self.time)) * self.L0
+
+        def forceSI():
+            return self.handle.indenter_force(plane.contactId) * (self.p0 * self.L0**2)
+
+        if record:
+            self.recordedQuantities.append(indentationSI)
+            self.recordedQuantities.append(forceSI)
+        return plane
+
+    def setInteractionSphere(self, record=True, isSpherical=True):
+        radius = self.parameters["SphereRadiusSI"] / self.L0
+        if isSpherical:
+            start = self.parameters["CELL"]["RadiusSIM"] + radius + self.parameters["InitialDistance"]
+        else:
+            start = self.cell.mesh.points[3][1] + radius + self.parameters["InitialDistance"]
+        v, tmove = self._move_params()
+        sphereFunc = _linear_schedule(start, v, tmove)
+        forceConst = 0.1
+        sphere = Sphere(radius, sphereFunc, forceConst)
+        self.register(sphere)
+
+        def indentationSI():
+            return (sphereFunc(0) - sphereFunc(self.time)) * self.L0
+
+        def forceSI():
+            return self.handle.indenter_force(sphere.contactId) * (self.p0 * self.L0**2)
+
+        if record:
+            self.recordedQuantities.append(indentationSI)
+            self.recordedQuantities.append(forceSI)
+        return sphere
+
+    def setInteractionTetra(self):
+        youngsModulusSI = self.parameters["CELL"]["YoungsModulusSI"]
+        poissonRatio = self.parameters["CELL"]["PoissonRatio"]
+        mooneyRivlinRatio = self.parameters["CELL"].get("MooneyRivlinRatio", 1)
+        youngsModulus = youngsModulusSI / self.p0
+        model = Tetra.materialModel[self.parameters["CELL"]["model"]]
+        self.register(Tetra(self.cell, youngsModulus, poissonRatio, mooneyRivlinRatio, model))
+
+    def setInteractionFiniteStrainViscoplastic(self):
+        """The viscoplastic material with the parameter mapping of the legacy driver
+        (SimulationLegacy.py:842-882): mu1 = r G, mu2 = (1-r) G, K, flowRate = T0,
+        yieldStress = timeConstantSI^(1/m) / YoungsScaling."""
+        c = self.parameters["CELL"]
+        youngsModulus = (c["YoungsModulusSI"] / self.parameters.get("ReynoldScaling", 1.0)
+                         / c.get("YoungsScaling", 1.0) / self.p0)
+        nu = c["PoissonRatio"]
+        r = c.get("MooneyRivlinRatio", 1.0)
+        G = youngsModulus / (2 * (1 + nu))
+        K = youngsModulus / (3 * (1 - 2 * nu))
+        m = c["ViscoplasticFlowExponent"]
+        yieldStress = c["ViscoplasticTimeConstantSI"] ** (1.0 / m) / c.get("YoungsScaling", 1.0)
+        self.register(FiniteStrainViscoplastic(r * G, (1 - r) * G, K, m, yieldStress, self.T0,
+                                               c["HardeningThreshhold"], c["HardeningExponent"]))
+
+    # Velocity Verlet last, as in the reference (Simulation.py:227)
+    def setInteractionVelocityVerlet(self, fixTopBottom=False, damping=0.005):
+        self.register(VelocityVerlet(self.numPoints, fixTopBottom, damping))
+
+    def _advance(self, n: int):
+        for interaction in self.interactions:
+            for t in range(self.time, self.time + n):
+                interaction.beforeTimeStep(t)
+            interaction.prepareSteps(self.time, n)
+        self.handle.step(n)
+        self.time += n
+
+    def timeStep(self):
+        self._advance(1)
+
+    def run(self, writeStress=True, writePressure=True, writeVolumeChange=False):
+        self._print(f"VTKInterval: {self.VTKInterval}")
+        starttimes, endtimes = [], []
+        numberCycles = self.parameters["VTKFramesTotal"]
+        writeVTK(self, writeStress=writeStress, writePressure=writePressure, writeVolumeChange=writeVolumeChange)
+        dataPoints = np.array([quant() for quant in self.recordedQuantities])
+        np.savetxt(self.parameters["OutputDir"] + "simdata.dat", dataPoints)
+        for i in range(numberCycles):
+            starttimes.append(time.time())
+            self._advance(self.VTKInterval)
+            self.handle.sync()
+            anatime1 = time.time()
+            writeVTK(self, writeStress=writeStress, writePressure=writePressure, writeVolumeChange=writeVolumeChange)
+            dataPoints = np.vstack((dataPoints, [quant() for quant in self.recordedQuantities]))
+            np.savetxt(self.parameters["OutputDir"] + "simdata.dat", dataPoints)
+            anatime2 = time.time()
+            endtimes.append(time.time())
+            cycleTime = np.average(np.array(endtimes) - np.array(starttimes))
+            self._print(f"| Average # of simulation steps per second: {np.round(self.VTKInterval / cycleTime, 1)} "
+                        f"| VTK cycle took {np.round(anatime2 - anatime1, 1)} seconds", end="\r")
+        self._print("")
+        return dataPoints
+
+    def close(self):
+        self.handle.close()

@@ -442,7 +442,7 @@ int nfx_set_record(nfx_sim* s, int contact, int64_t every, int64_t max_rows) {
     s->prm.record_contact = contact;
     s->prm.record_every = contact >= 0 ? every : 0;
     s->prm.max_rows = contact >= 0 ? max_rows : 0;
-    s->prm.fields_every = contact >= 0 ? every : 0;
+    s->prm.fields_every = every > 0 ? every : 0;
     s->rows_written = 0;
     invalidate_graph(s);
     return NFX_OK;

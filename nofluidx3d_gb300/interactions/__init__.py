@@ -1,0 +1,9 @@
+from nofluidx3d_gb300.interactions.FiniteStrainViscoplastic import FiniteStrainViscoplastic
+from nofluidx3d_gb300.interactions.Interaction import Interaction
+from nofluidx3d_gb300.interactions.Plane import Plane
+from nofluidx3d_gb300.interactions.Sphere import Sphere
+from nofluidx3d_gb300.interactions.Substrate import Substrate
+from nofluidx3d_gb300.interactions.Tetra import Tetra
+from nofluidx3d_gb300.interactions.VelocityVerlet import VelocityVerlet
+
+__all__ = ["FiniteStrainViscoplastic", "Interaction", "Plane", "Sphere", "Substrate", "Tetra", "VelocityVerlet"]
