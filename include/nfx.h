@@ -173,6 +173,30 @@ int nfx_profile_steps(nfx_sim* sim, int64_t nsteps, float* tet_ms, float* node_m
 /* Number of mesh tiles and distinct-node entries (diagnostics for the tile layout). */
 int nfx_mesh_info(nfx_sim* sim, int64_t* ntiles, int64_t* tile_nodes);
 
+/* Indenter force of one contact on node positions the caller keeps in device memory, written
+ * to one double in device memory. This entry point has no counterpart in the reference.
+ *
+ * It is for callers that cannot allocate device memory: a host solver that reserves its whole
+ * device budget in its own pool at start-up and forbids any later cudaMalloc, or a coupling
+ * loop that must not allocate (nor wait for the device synchronisation an allocation may bring)
+ * between time steps. It allocates nothing. The per-block partial sums and the completion
+ * counter of its fixed-order reduction live in one static device array of 128 KiB, which every
+ * GPU that loads this library holds until the process exits; np is therefore limited to
+ * NFX_NOALLOC_MAX_NODES, and a larger np returns NFX_ERR_ARG.
+ *
+ * The first call on a device looks up the array's device address with that device current;
+ * make that first call before any stream capture. Every call shares the array, and it keeps
+ * the last call's contents (the counter is cleared at the start of each call): calls whose
+ * work overlaps on the GPU — on different streams with no ordering between them — race and
+ * give wrong results.
+ *
+ * points_dev: double[3*np] SoA in device memory; kind/k/radius as nfx_add_contact; position:
+ * the contact's current position (plane/substrate height, sphere centre y); out_dev: one double
+ * in device memory; stream: a cudaStream_t (NULL = the legacy default stream). Same contact laws
+ * and sign as nfx_indenter_force. Errors are reported through nfx_last_error. */
+#define NFX_NOALLOC_MAX_NODES 4194304
+int nfx_indenter_force_noalloc(int device, int64_t np, const double* points_dev, int kind, double k, double radius,
+                               double position, double* out_dev, void* stream);
 
 #ifdef __cplusplus
 }

@@ -39,6 +39,8 @@ constexpr int GRAPH_STEPS = 100;  // steps per captured CUDA graph chunk
 
 }  // namespace
 
+void nfx::set_error(const std::string& msg) { g_err = msg; }
+
 struct nfx_sim {
     int device = 0;
     cudaStream_t stream = nullptr;

@@ -110,6 +110,9 @@ struct StepParams {
     int fix_a, fix_b;          // internal ids of the pinned nodes, -1 if none
 };
 
+// Sets the message nfx_last_error() returns on this thread (nfx_api.cpp).
+void set_error(const std::string& msg);
+
 // Kernel launchers (nfx_kernels.cu). All enqueue on `stream` and return cudaGetLastError().
 cudaError_t launch_tet_pass(const MeshDev& m, const StateDev& s, const MaterialDev& mat, const StepParams& p,
                             int t_offset, cudaStream_t stream);
