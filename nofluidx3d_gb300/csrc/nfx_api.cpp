@@ -236,14 +236,15 @@ int nfx_set_mesh(nfx_sim* s, int64_t np, int64_t nt, const double* points, const
     s->plan = std::move(plan);
     const MeshPlan& P = s->plan;
     auto& A = s->mesh_allocs;
-    int* tb; int* nbg; unsigned* tn; uchar4* lc; float4 *da, *db; float2* dc; float4 *xh, *xl;
-    float4 *uh, *ul, *v, *fo, *fa; double* part;
+    int* tb; int* nbg; uint2* tn; uchar4* lc; ushort4* ti; float4 *da, *db; float2* dc; float4 *xh, *xl;
+    float4 *uh, *ul, *v, *fo; unsigned long long* fa; double* part;
     if ((rc = dalloc(s, &tb, P.tile_tet_begin.size(), &A)) || (rc = dalloc(s, &nbg, P.tile_node_begin.size(), &A)) ||
-        (rc = dalloc(s, &tn, P.tile_nodes.size(), &A)) || (rc = dalloc(s, &lc, (size_t)nt, &A)) ||
+        (rc = dalloc(s, &tn, P.tile_nodes.size() / 2, &A)) || (rc = dalloc(s, &lc, (size_t)nt, &A)) ||
+        (rc = dalloc(s, &ti, (size_t)nt, &A)) ||
         (rc = dalloc(s, &da, (size_t)nt, &A)) || (rc = dalloc(s, &db, (size_t)nt, &A)) || (rc = dalloc(s, &dc, (size_t)nt, &A)) ||
         (rc = dalloc(s, &xh, (size_t)np, &A)) || (rc = dalloc(s, &xl, (size_t)np, &A)) || (rc = dalloc(s, &uh, (size_t)np, &A)) ||
         (rc = dalloc(s, &ul, (size_t)np, &A)) || (rc = dalloc(s, &v, (size_t)np, &A)) || (rc = dalloc(s, &fo, (size_t)np, &A)) ||
-        (rc = dalloc(s, &fa, (size_t)np, &A)) || (rc = dalloc(s, &part, (size_t)((np + NODE_BLOCK - 1) / NODE_BLOCK), &A)) ||
+        (rc = dalloc(s, &fa, 3 * (size_t)np, &A)) || (rc = dalloc(s, &part, (size_t)((np + NODE_BLOCK - 1) / NODE_BLOCK), &A)) ||
         (rc = dalloc(s, &s->d_node_user, (size_t)np, &A)) || (rc = dalloc(s, &s->d_stage, 9 * (size_t)std::max(np, nt), &A))) {
         free_mesh(s);
         return rc;
@@ -263,13 +264,15 @@ int nfx_set_mesh(nfx_sim* s, int64_t np, int64_t nt, const double* points, const
     CUDA_TRY(cudaMemcpyAsync(nbg, P.tile_node_begin.data(), P.tile_node_begin.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(tn, P.tile_nodes.data(), P.tile_nodes.size() * sizeof(unsigned), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(lc, P.lconn.data(), P.lconn.size(), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(ti, P.tile_inc.data(), P.tile_inc.size() * sizeof(uint16_t), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(da, a.data(), a.size() * sizeof(float), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(db, b.data(), b.size() * sizeof(float), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(dc, c.data(), c.size() * sizeof(float), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(xh, P.Xh.data(), P.Xh.size() * sizeof(float), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(xl, P.Xl.data(), P.Xl.size() * sizeof(float), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(s->d_node_user, nu.data(), nu.size() * sizeof(long long), cudaMemcpyHostToDevice, st));
-    for (float4* z : {uh, ul, v, fo, fa}) CUDA_TRY(cudaMemsetAsync(z, 0, (size_t)np * sizeof(float4), st));
+    for (float4* z : {uh, ul, v, fo}) CUDA_TRY(cudaMemsetAsync(z, 0, (size_t)np * sizeof(float4), st));
+    CUDA_TRY(cudaMemsetAsync(fa, 0, 3 * (size_t)np * sizeof(unsigned long long), st));
     CUDA_TRY(cudaMemsetAsync(s->d_time, 0, sizeof(long long), st));
     CUDA_TRY(cudaMemsetAsync(s->d_status, 0, sizeof(unsigned), st));
     CUDA_TRY(cudaStreamSynchronize(st));  // host vectors a/b/c/nu go out of scope
@@ -280,6 +283,7 @@ int nfx_set_mesh(nfx_sim* s, int64_t np, int64_t nt, const double* points, const
     s->mesh.tile_node_begin = nbg;
     s->mesh.tile_nodes = tn;
     s->mesh.lconn = lc;
+    s->mesh.tile_inc = ti;
     s->mesh.dmi_a = da;
     s->mesh.dmi_b = db;
     s->mesh.dmi_c = dc;
@@ -687,7 +691,7 @@ int nfx_mesh_info(nfx_sim* s, int64_t* ntiles, int64_t* tile_nodes) {
     CHECK_ARG(s && ntiles && tile_nodes, "null argument");
     if (!s->have_mesh) return fail(NFX_ERR_STATE, "no mesh");
     *ntiles = s->plan.ntiles;
-    *tile_nodes = (int64_t)s->plan.tile_nodes.size();
+    *tile_nodes = (int64_t)s->plan.tile_nodes.size() / 2;
     return NFX_OK;
 }
 

@@ -20,6 +20,11 @@ constexpr int TILE_TETS = 256;
 constexpr int TILE_NODES_MAX = 256;
 constexpr int NODE_BLOCK = 256;
 
+// Fixed-point scale of the force accumulator: 2^40 (resolution 9.1e-13, range +-8.4e6).
+constexpr float FORCE_FIX_SCALE = 1099511627776.0f;
+constexpr float FORCE_FIX_INV = 1.0f / 1099511627776.0f;
+constexpr float FORCE_FIX_MAX = 4.0e6f;  // larger tile sums raise STATUS_NONFINITE
+
 // Status bits raised by the kernels (read back by nfx_status).
 constexpr unsigned STATUS_NONFINITE = 1u;   // a position or force became NaN/Inf
 constexpr unsigned STATUS_INVERTED = 2u;    // an element reached det F <= 0
@@ -35,8 +40,11 @@ struct MeshPlan {
     std::vector<int64_t> tet_user;    // internal tetra -> user tetra id
     std::vector<int32_t> tile_tet_begin;   // ntiles + 1
     std::vector<int32_t> tile_node_begin;  // ntiles + 1
-    std::vector<uint32_t> tile_nodes;      // internal node ids, sorted within a tile
+    std::vector<uint32_t> tile_nodes;      // 2 per tile node: internal node id, (first << 16 | count)
+                                           // of its run in the tile's incidence list
     std::vector<uint8_t> lconn;            // 4 * nt local corner indices (internal tet order)
+    std::vector<uint16_t> tile_inc;        // 4 * nt: per tile, the corners (4*local tet + corner)
+                                           // grouped by local node in node order, tet order within
     std::vector<float> dmi;                // 12 * nt: Dm^-1 row-major (9), V0, pad, pad
     std::vector<float> Xh, Xl;             // 4 * np: reference position hi / lo parts
 };
@@ -53,8 +61,9 @@ struct MeshDev {
     int np, nt, ntiles;
     const int* tile_tet_begin;
     const int* tile_node_begin;
-    const unsigned* tile_nodes;
+    const uint2* tile_nodes;   // (node id, first << 16 | count)
     const uchar4* lconn;
+    const ushort4* tile_inc;   // four incidence entries per tetra slot of the tile
     const float4* dmi_a;  // Dm^-1 entries 0..3
     const float4* dmi_b;  // Dm^-1 entries 4..7
     const float2* dmi_c;  // Dm^-1 entry 8, V0
@@ -67,7 +76,10 @@ struct StateDev {
     float4* ul;     // displacement lo
     float4* v;      // velocity
     float4* fo;     // force of the previous step
-    float4* facc;   // element-force accumulator (zeroed by the node pass)
+    // Element-force accumulator, 3 * np signed 64-bit fixed-point values (component d of node
+    // i at [d*np + i], FORCE_FIX_SCALE units per force unit), zeroed by the node pass. Integer
+    // addition is associative, so the sum does not depend on the order of the atomics.
+    unsigned long long* facc;
     float4* vp_a;   // viscoplastic P = Fp - I, entries 0..3
     float4* vp_b;   // entries 4..7
     float2* vp_c;   // entry 8, accumulated plastic strain

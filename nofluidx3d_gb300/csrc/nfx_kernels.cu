@@ -43,7 +43,8 @@ __global__ void __launch_bounds__(TILE_TETS) k_tet_pass(MeshDev m, StateDev s, M
                                                         long long fields_every, int t_offset) {
     __shared__ float4 s_uh[TILE_NODES_MAX];
     __shared__ float4 s_ul[TILE_NODES_MAX];
-    __shared__ float s_f[3 * TILE_NODES_MAX];
+    __shared__ float4 s_cf[4 * TILE_TETS];      // corner forces, slot 4*local tet + corner
+    __shared__ ushort4 s_inc[TILE_TETS];        // the tile's incidence list
 
     const int b = blockIdx.x;
     const int j = threadIdx.x;
@@ -70,15 +71,13 @@ __global__ void __launch_bounds__(TILE_TETS) k_tet_pass(MeshDev m, StateDev s, M
             pb = __ldcs(s.vp_b + t);
             pc = __ldcs(s.vp_c + t);
         }
+        s_inc[j] = __ldcs(m.tile_inc + t);
     }
-    unsigned g = 0;
+    uint2 node = make_uint2(0u, 0u);
     if (j < nn) {
-        g = m.tile_nodes[nb + j];
-        s_uh[j] = s.uh[g];
-        s_ul[j] = s.ul[g];
-        s_f[j] = 0.f;
-        s_f[TILE_NODES_MAX + j] = 0.f;
-        s_f[2 * TILE_NODES_MAX + j] = 0.f;
+        node = m.tile_nodes[nb + j];
+        s_uh[j] = s.uh[node.x];
+        s_ul[j] = s.ul[node.x];
     }
     __syncthreads();
 
@@ -129,19 +128,31 @@ __global__ void __launch_bounds__(TILE_TETS) k_tet_pass(MeshDev m, StateDev s, M
             }
         }
         if (!(jm1 > -1.0f)) atomicOr(s.status, STATUS_INVERTED);
-        const float chk = (f[0][0] + f[1][0]) + (f[2][0] + f[3][0]) + f[0][1] + f[1][2] + f[2][1] + f[3][2];
-        if (!isfinite(chk)) atomicOr(s.status, STATUS_NONFINITE);
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
-            atomicAdd(&s_f[li[k]], f[k][0]);
-            atomicAdd(&s_f[TILE_NODES_MAX + li[k]], f[k][1]);
-            atomicAdd(&s_f[2 * TILE_NODES_MAX + li[k]], f[k][2]);
-        }
+        for (int k = 0; k < 4; k++) s_cf[4 * j + k] = make_float4(f[k][0], f[k][1], f[k][2], 0.f);
     }
     __syncthreads();
+    // Each tile node sums its corner forces in the tile's fixed incidence order, then adds the
+    // sum to the global accumulator as 64-bit fixed point: the total is independent of the
+    // order in which tiles finish.
     if (j < nn) {
-        const float4 acc = make_float4(s_f[j], s_f[TILE_NODES_MAX + j], s_f[2 * TILE_NODES_MAX + j], 0.f);
-        atomicAdd(s.facc + g, acc);
+        const unsigned first = node.y >> 16, count = node.y & 0xffffu;
+        const unsigned short* inc = reinterpret_cast<const unsigned short*>(s_inc);
+        float fx = 0.f, fy = 0.f, fz = 0.f;
+        for (unsigned q = 0; q < count; q++) {
+            const float4 c = s_cf[inc[first + q]];
+            fx += c.x;
+            fy += c.y;
+            fz += c.z;
+        }
+        if (!(fabsf(fx) <= FORCE_FIX_MAX && fabsf(fy) <= FORCE_FIX_MAX && fabsf(fz) <= FORCE_FIX_MAX)) {
+            atomicOr(s.status, STATUS_NONFINITE);
+        } else {
+            const long long np = m.np;
+            atomicAdd(s.facc + node.x, (unsigned long long)__float2ll_rn(fx * FORCE_FIX_SCALE));
+            atomicAdd(s.facc + np + node.x, (unsigned long long)__float2ll_rn(fy * FORCE_FIX_SCALE));
+            atomicAdd(s.facc + 2 * np + node.x, (unsigned long long)__float2ll_rn(fz * FORCE_FIX_SCALE));
+        }
     }
 }
 
@@ -260,7 +271,10 @@ __global__ void __launch_bounds__(NODE_BLOCK) k_node_pass(MeshDev m, StateDev s,
     }
     double ro = 0.0;
     if (i < m.np) {
-        float4 f = s.facc[i];
+        const long long np = m.np;
+        float4 f = make_float4(__ll2float_rn((long long)s.facc[i]) * FORCE_FIX_INV,
+                               __ll2float_rn((long long)s.facc[np + i]) * FORCE_FIX_INV,
+                               __ll2float_rn((long long)s.facc[2 * np + i]) * FORCE_FIX_INV, 0.f);
         const float4 xh = m.Xh[i], xl = m.Xl[i];
         float4 uh = s.uh[i], ul = s.ul[i];
         for (int c = 0; c < p.n_contacts; c++) {
@@ -288,7 +302,9 @@ __global__ void __launch_bounds__(NODE_BLOCK) k_node_pass(MeshDev m, StateDev s,
             s.ul[i] = ul;
             s.v[i] = v;
             s.fo[i] = make_float4(f.x, f.y, f.z, 0.f);
-            s.facc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+            s.facc[i] = 0ull;
+            s.facc[np + i] = 0ull;
+            s.facc[2 * np + i] = 0ull;
         }
     }
     if (rec) {

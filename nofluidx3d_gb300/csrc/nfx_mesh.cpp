@@ -120,6 +120,7 @@ bool build_mesh_plan(int64_t np, int64_t nt, const double* P, const uint32_t* T,
 
     // tiles
     plan.lconn.resize(4 * (size_t)nt);
+    plan.tile_inc.resize(4 * (size_t)nt);
     plan.tile_tet_begin.push_back(0);
     plan.tile_node_begin.push_back(0);
     std::vector<uint32_t> ids;
@@ -138,18 +139,32 @@ bool build_mesh_plan(int64_t np, int64_t nt, const double* P, const uint32_t* T,
             if ((int64_t)ids.size() <= TILE_NODES_MAX || cnt == 1) break;
             cnt = std::max<int64_t>(1, cnt - 16);
         }
+        const size_t nn = ids.size();
+        std::vector<uint32_t> count(nn, 0), first(nn, 0);
         for (int64_t j = 0; j < cnt; j++) {
             const int64_t ut = plan.tet_user[t0 + j];
             for (int k = 0; k < 4; k++) {
                 const uint32_t g = (uint32_t)plan.node_int[T[k * nt + ut]];
                 const size_t loc = std::lower_bound(ids.begin(), ids.end(), g) - ids.begin();
                 plan.lconn[4 * (t0 + j) + k] = (uint8_t)loc;
+                count[loc]++;
             }
         }
-        plan.tile_nodes.insert(plan.tile_nodes.end(), ids.begin(), ids.end());
+        // incidence list of the tile: corners grouped by local node, in (tet, corner) order
+        for (size_t q = 1; q < nn; q++) first[q] = first[q - 1] + count[q - 1];
+        std::vector<uint32_t> fill(first);
+        for (int64_t j = 0; j < cnt; j++)
+            for (int k = 0; k < 4; k++) {
+                const uint8_t loc = plan.lconn[4 * (t0 + j) + k];
+                plan.tile_inc[4 * t0 + fill[loc]++] = (uint16_t)(4 * j + k);
+            }
+        for (size_t q = 0; q < nn; q++) {
+            plan.tile_nodes.push_back(ids[q]);
+            plan.tile_nodes.push_back((first[q] << 16) | count[q]);
+        }
         t0 += cnt;
         plan.tile_tet_begin.push_back((int32_t)t0);
-        plan.tile_node_begin.push_back((int32_t)plan.tile_nodes.size());
+        plan.tile_node_begin.push_back((int32_t)(plan.tile_nodes.size() / 2));
     }
     plan.ntiles = (int64_t)plan.tile_tet_begin.size() - 1;
 

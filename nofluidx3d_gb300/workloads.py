@@ -128,4 +128,11 @@ def plain_large_1m() -> Workload:
     return plain_large().with_(name="plain-large R34 MR+VP sphere", radius=34.0)
 
 
-WORKLOADS = {"plain-small": plain_small, "plain-large": plain_large, "plain-large-1m": plain_large_1m}
+def plain_large_r48() -> Workload:
+    """The same construction at R = 48 (2,778,816 tetra): large enough that one step's
+    viscoplastic state (~350 MB read + written) exceeds L2, small enough for full ncu captures."""
+    return plain_large().with_(name="plain-large R48 MR+VP sphere", radius=48.0)
+
+
+WORKLOADS = {"plain-small": plain_small, "plain-large": plain_large, "plain-large-1m": plain_large_1m,
+             "plain-large-r48": plain_large_r48}
