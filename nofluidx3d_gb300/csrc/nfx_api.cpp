@@ -68,6 +68,9 @@ struct nfx_sim {
     long long time = 0;          // host mirror of the device time
     cudaGraphExec_t graph = nullptr;
     bool graph_valid = false;
+    int sm_count = 1;
+    int tet_variant = 1;                   // 1: persistent pipelined element pass, 0: one CTA per tile
+    int pipe_bps[4] = {-1, -1, -1, -1};    // resident CTAs per SM of the pipelined kernel, per model
 };
 
 namespace {
@@ -116,9 +119,24 @@ int require_ready(nfx_sim* s) {
     return NFX_OK;
 }
 
+// Element pass launch: the persistent pipelined kernel on a grid of (resident CTAs per SM) x
+// (SM count), capped at the tile count; the one-CTA-per-tile kernel when selected
+// (NFX_TET_KERNEL=0 in the environment) or when the pipelined kernel cannot be resident.
+cudaError_t launch_elem(nfx_sim* s, int k) {
+    if (s->tet_variant == 1) {
+        int& bps = s->pipe_bps[s->mat.model & 3];
+        if (bps < 0) bps = pipe_blocks_per_sm(s->mat.model);
+        if (bps > 0) {
+            const long long grid = std::min<long long>((long long)bps * s->sm_count, s->mesh.ntiles);
+            return launch_tet_pass_pipe(s->mesh, s->st, s->mat, s->prm, k, (int)grid, s->stream);
+        }
+    }
+    return launch_tet_pass(s->mesh, s->st, s->mat, s->prm, k, s->stream);
+}
+
 int enqueue_steps(nfx_sim* s, int n) {
     for (int k = 0; k < n; k++) {
-        CUDA_TRY(launch_tet_pass(s->mesh, s->st, s->mat, s->prm, k, s->stream));
+        CUDA_TRY(launch_elem(s, k));
         CUDA_TRY(launch_node_pass(s->mesh, s->st, s->prm, k, NODE_UPDATE, -1, s->stream));
     }
     CUDA_TRY(launch_advance_time(s->st, n, s->stream));
@@ -193,6 +211,9 @@ int nfx_create(int device, nfx_sim** out) {
     s->st.force_out = s->d_force_out;
     s->prm.record_contact = -1;
     s->prm.fix_a = s->prm.fix_b = -1;
+    cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (s->sm_count < 1) s->sm_count = 1;
+    if (const char* v = std::getenv("NFX_TET_KERNEL")) s->tet_variant = std::atoi(v) == 0 ? 0 : 1;
     // default integrator: the reference's xi = 0.005 (VelocityVerlet.cl:11)
     const double xi = 0.005;
     s->prm.vv_a = (float)((1 - 0.5 * xi) / (1 + 0.5 * xi));
@@ -238,10 +259,11 @@ int nfx_set_mesh(nfx_sim* s, int64_t np, int64_t nt, const double* points, const
     auto& A = s->mesh_allocs;
     int* tb; int* nbg; uint2* tn; uchar4* lc; ushort4* ti; float4 *da, *db; float2* dc; float4 *xh, *xl;
     float4 *uh, *ul, *v, *fo; unsigned long long* fa; double* part;
+    const size_t ntp = (size_t)nt + ARRAY_PAD;  // per-tetra arrays carry ARRAY_PAD zeroed elements
     if ((rc = dalloc(s, &tb, P.tile_tet_begin.size(), &A)) || (rc = dalloc(s, &nbg, P.tile_node_begin.size(), &A)) ||
-        (rc = dalloc(s, &tn, P.tile_nodes.size() / 2, &A)) || (rc = dalloc(s, &lc, (size_t)nt, &A)) ||
-        (rc = dalloc(s, &ti, (size_t)nt, &A)) ||
-        (rc = dalloc(s, &da, (size_t)nt, &A)) || (rc = dalloc(s, &db, (size_t)nt, &A)) || (rc = dalloc(s, &dc, (size_t)nt, &A)) ||
+        (rc = dalloc(s, &tn, P.tile_nodes.size() / 2 + ARRAY_PAD, &A)) || (rc = dalloc(s, &lc, ntp, &A)) ||
+        (rc = dalloc(s, &ti, ntp, &A)) ||
+        (rc = dalloc(s, &da, ntp, &A)) || (rc = dalloc(s, &db, ntp, &A)) || (rc = dalloc(s, &dc, ntp, &A)) ||
         (rc = dalloc(s, &xh, (size_t)np, &A)) || (rc = dalloc(s, &xl, (size_t)np, &A)) || (rc = dalloc(s, &uh, (size_t)np, &A)) ||
         (rc = dalloc(s, &ul, (size_t)np, &A)) || (rc = dalloc(s, &v, (size_t)np, &A)) || (rc = dalloc(s, &fo, (size_t)np, &A)) ||
         (rc = dalloc(s, &fa, 3 * (size_t)np, &A)) || (rc = dalloc(s, &part, (size_t)((np + NODE_BLOCK - 1) / NODE_BLOCK), &A)) ||
@@ -260,6 +282,13 @@ int nfx_set_mesh(nfx_sim* s, int64_t np, int64_t nt, const double* points, const
     }
     std::vector<long long> nu(P.node_user.begin(), P.node_user.end());
     cudaStream_t st = s->stream;
+    // zero the padding so bulk copies past a tile's end read defined values
+    CUDA_TRY(cudaMemsetAsync(tn, 0, (P.tile_nodes.size() / 2 + ARRAY_PAD) * sizeof(uint2), st));
+    CUDA_TRY(cudaMemsetAsync(lc, 0, ntp * sizeof(uchar4), st));
+    CUDA_TRY(cudaMemsetAsync(ti, 0, ntp * sizeof(ushort4), st));
+    CUDA_TRY(cudaMemsetAsync(da, 0, ntp * sizeof(float4), st));
+    CUDA_TRY(cudaMemsetAsync(db, 0, ntp * sizeof(float4), st));
+    CUDA_TRY(cudaMemsetAsync(dc, 0, ntp * sizeof(float2), st));
     CUDA_TRY(cudaMemcpyAsync(tb, P.tile_tet_begin.data(), P.tile_tet_begin.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(nbg, P.tile_node_begin.data(), P.tile_node_begin.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(tn, P.tile_nodes.data(), P.tile_nodes.size() * sizeof(unsigned), cudaMemcpyHostToDevice, st));
@@ -334,16 +363,16 @@ int nfx_set_viscoplastic(nfx_sim* s, const double* par) {
     CHECK_ARG(par[6] != 0, "hardening threshold must be non-zero");
     int rc;
     if ((rc = set_device(s)) != NFX_OK) return rc;
-    const int64_t nt = s->plan.nt;
+    const size_t ntp = (size_t)s->plan.nt + ARRAY_PAD;
     if (!s->st.vp_a) {
-        if ((rc = dalloc(s, &s->st.vp_a, (size_t)nt, &s->mesh_allocs)) || (rc = dalloc(s, &s->st.vp_b, (size_t)nt, &s->mesh_allocs)) ||
-            (rc = dalloc(s, &s->st.vp_c, (size_t)nt, &s->mesh_allocs)) || (rc = dalloc(s, &s->st.fields, (size_t)nt, &s->mesh_allocs)))
+        if ((rc = dalloc(s, &s->st.vp_a, ntp, &s->mesh_allocs)) || (rc = dalloc(s, &s->st.vp_b, ntp, &s->mesh_allocs)) ||
+            (rc = dalloc(s, &s->st.vp_c, ntp, &s->mesh_allocs)) || (rc = dalloc(s, &s->st.fields, ntp, &s->mesh_allocs)))
             return rc;
     }
-    CUDA_TRY(cudaMemsetAsync(s->st.vp_a, 0, (size_t)nt * sizeof(float4), s->stream));
-    CUDA_TRY(cudaMemsetAsync(s->st.vp_b, 0, (size_t)nt * sizeof(float4), s->stream));
-    CUDA_TRY(cudaMemsetAsync(s->st.vp_c, 0, (size_t)nt * sizeof(float2), s->stream));
-    CUDA_TRY(cudaMemsetAsync(s->st.fields, 0, (size_t)nt * sizeof(float2), s->stream));
+    CUDA_TRY(cudaMemsetAsync(s->st.vp_a, 0, ntp * sizeof(float4), s->stream));
+    CUDA_TRY(cudaMemsetAsync(s->st.vp_b, 0, ntp * sizeof(float4), s->stream));
+    CUDA_TRY(cudaMemsetAsync(s->st.vp_c, 0, ntp * sizeof(float2), s->stream));
+    CUDA_TRY(cudaMemsetAsync(s->st.fields, 0, ntp * sizeof(float2), s->stream));
     s->mat = MaterialDev{};
     s->mat.model = MODEL_VP;
     s->mat.mu1 = (float)par[0];
@@ -663,7 +692,7 @@ int nfx_profile_steps(nfx_sim* s, int64_t nsteps, float* tet_ms, float* node_ms)
     cudaError_t err = cudaSuccess;
     for (int64_t k = 0; k < nsteps && err == cudaSuccess; k++) {
         cudaEventRecord(ev[3 * k], s->stream);
-        err = launch_tet_pass(s->mesh, s->st, s->mat, s->prm, (int)k, s->stream);
+        err = launch_elem(s, (int)k);
         cudaEventRecord(ev[3 * k + 1], s->stream);
         if (err == cudaSuccess) err = launch_node_pass(s->mesh, s->st, s->prm, (int)k, NODE_UPDATE, -1, s->stream);
         cudaEventRecord(ev[3 * k + 2], s->stream);

@@ -29,6 +29,11 @@ constexpr float FORCE_FIX_MAX = 4.0e6f;  // larger tile sums raise STATUS_NONFIN
 constexpr unsigned STATUS_NONFINITE = 1u;   // a position or force became NaN/Inf
 constexpr unsigned STATUS_INVERTED = 2u;    // an element reached det F <= 0
 constexpr unsigned STATUS_CURVE_FULL = 4u;  // a record row fell outside the curve buffer
+constexpr unsigned STATUS_TIMEOUT = 8u;     // a bounded wait on an asynchronous copy gave up
+
+// Extra elements allocated after every per-tetra array and the tile node list: bulk copies
+// round their sizes up to 16 bytes and may read that far past a tile's last element.
+constexpr int ARRAY_PAD = 16;
 
 // ---------------------------------------------------------------------------------------
 // Host-side mesh plan: reordering, tiles, per-tetra reference quantities.
@@ -128,6 +133,11 @@ void set_error(const std::string& msg);
 // Kernel launchers (nfx_kernels.cu). All enqueue on `stream` and return cudaGetLastError().
 cudaError_t launch_tet_pass(const MeshDev& m, const StateDev& s, const MaterialDev& mat, const StepParams& p,
                             int t_offset, cudaStream_t stream);
+// Persistent, bulk-copy-pipelined element pass: `grid` CTAs walk all tiles.
+cudaError_t launch_tet_pass_pipe(const MeshDev& m, const StateDev& s, const MaterialDev& mat, const StepParams& p,
+                                 int t_offset, int grid, cudaStream_t stream);
+// Resident CTAs per SM of the pipelined element pass for a material model (0 on error).
+int pipe_blocks_per_sm(int model);
 enum NodeMode : int { NODE_UPDATE = 0, NODE_READOUT_ROW = 1, NODE_READOUT_VALUE = 2 };
 cudaError_t launch_node_pass(const MeshDev& m, const StateDev& s, const StepParams& p, int t_offset, int mode,
                              int readout_contact, cudaStream_t stream);

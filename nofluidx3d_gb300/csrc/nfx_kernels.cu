@@ -36,15 +36,103 @@ __device__ __forceinline__ double contact_pos(const ContactDev& c, long long t) 
 }
 
 // ------------------------------------------------------------------------------------------
-// Element pass
+// Element pass: shared pieces
+// ------------------------------------------------------------------------------------------
+
+// One tetra: displacement differences from the tile's staged node data, the material law, the
+// viscoplastic state update (written back with evict-first stores), the four corner forces
+// into the shared corner-force slots 4*j .. 4*j+3.
+template <int MODEL>
+__device__ __forceinline__ void element_eval(int j, long long t, uchar4 lc, float4 da, float4 db, float2 dc,
+                                             float4 pa, float4 pb, float2 pc, const float4* s_uh,
+                                             const float4* s_ul, float4* s_cf, const StateDev& s,
+                                             const MaterialDev& mat, bool write_fields) {
+    const int li[4] = {lc.x, lc.y, lc.z, lc.w};
+    const float4 u0h = s_uh[li[0]], u0l = s_ul[li[0]];
+    float d[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const float4 h = s_uh[li[k + 1]], l = s_ul[li[k + 1]];
+        d[k][0] = (h.x - u0h.x) + (l.x - u0l.x);
+        d[k][1] = (h.y - u0h.y) + (l.y - u0l.y);
+        d[k][2] = (h.z - u0h.z) + (l.z - u0l.z);
+    }
+    const float Dmi[9] = {da.x, da.y, da.z, da.w, db.x, db.y, db.z, db.w, dc.x};
+    const float V0 = dc.y;
+    float f[4][3];
+    float jm1;
+    if (MODEL == MODEL_MR) {
+        jm1 = mr_element(d[0], d[1], d[2], Dmi, V0, mat.mu1, mat.mu2, mat.kappa, f);
+    } else if (MODEL == MODEL_SVK) {
+        jm1 = svk_element(d[0], d[1], d[2], Dmi, V0, mat.mu, mat.kp, f);
+    } else if (MODEL == MODEL_SVKK) {
+        jm1 = svkk_element(d[0], d[1], d[2], Dmi, V0, mat.mu, mat.kp, f);
+    } else {
+        VPParams par;
+        par.mu1 = mat.mu1;
+        par.mu2 = mat.mu2;
+        par.kappa = mat.kappa;
+        par.flow_exp = mat.flow_exp;
+        par.yield = mat.yield;
+        par.flow_rate = mat.flow_rate;
+        par.hard_thr = mat.hard_thr;
+        par.hard_exp = mat.hard_exp;
+        float P[9] = {pa.x, pa.y, pa.z, pa.w, pb.x, pb.y, pb.z, pb.w, pc.x};
+        float eps = pc.y;
+        float dP[9], rate, vm, pr;
+        vp_element(d[0], d[1], d[2], Dmi, V0, par, P, eps, dP, rate, f, vm, pr, jm1);
+#pragma unroll
+        for (int q = 0; q < 9; q++) P[q] += dP[q];
+        eps += rate;
+        __stcs(s.vp_a + t, make_float4(P[0], P[1], P[2], P[3]));
+        __stcs(s.vp_b + t, make_float4(P[4], P[5], P[6], P[7]));
+        __stcs(s.vp_c + t, make_float2(P[8], eps));
+        if (write_fields) __stcs(s.fields + t, make_float2(vm, pr));
+    }
+    if (!(jm1 > -1.0f)) atomicOr(s.status, STATUS_INVERTED);
+#pragma unroll
+    for (int k = 0; k < 4; k++) s_cf[4 * j + k] = make_float4(f[k][0], f[k][1], f[k][2], 0.f);
+}
+
+// One tile node: sum its corner forces in the tile's fixed incidence order and add the sum to
+// the global accumulator as 64-bit fixed point, so the total does not depend on the order in
+// which tiles finish.
+__device__ __forceinline__ void node_flush(uint2 node, const unsigned short* inc, const float4* s_cf,
+                                           const StateDev& s, long long np) {
+    const unsigned first = node.y >> 16, count = node.y & 0xffffu;
+    if (count == 0) return;
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    for (unsigned q = 0; q < count; q++) {
+        const float4 c = s_cf[inc[first + q]];
+        fx += c.x;
+        fy += c.y;
+        fz += c.z;
+    }
+    if (!(fabsf(fx) <= FORCE_FIX_MAX && fabsf(fy) <= FORCE_FIX_MAX && fabsf(fz) <= FORCE_FIX_MAX)) {
+        atomicOr(s.status, STATUS_NONFINITE);
+        return;
+    }
+    atomicAdd(s.facc + node.x, (unsigned long long)__float2ll_rn(fx * FORCE_FIX_SCALE));
+    atomicAdd(s.facc + np + node.x, (unsigned long long)__float2ll_rn(fy * FORCE_FIX_SCALE));
+    atomicAdd(s.facc + 2 * np + node.x, (unsigned long long)__float2ll_rn(fz * FORCE_FIX_SCALE));
+}
+
+__device__ __forceinline__ bool fields_due(const StateDev& s, long long fields_every, int t_offset) {
+    if (fields_every <= 0) return false;
+    const long long tt = *s.time + t_offset;
+    return (tt + 1) % fields_every == 0;
+}
+
+// ------------------------------------------------------------------------------------------
+// Element pass, one CTA per tile (plain loads)
 // ------------------------------------------------------------------------------------------
 template <int MODEL>
 __global__ void __launch_bounds__(TILE_TETS) k_tet_pass(MeshDev m, StateDev s, MaterialDev mat,
                                                         long long fields_every, int t_offset) {
     __shared__ float4 s_uh[TILE_NODES_MAX];
     __shared__ float4 s_ul[TILE_NODES_MAX];
-    __shared__ float4 s_cf[4 * TILE_TETS];      // corner forces, slot 4*local tet + corner
-    __shared__ ushort4 s_inc[TILE_TETS];        // the tile's incidence list
+    __shared__ float4 s_cf[4 * TILE_TETS];  // corner forces, slot 4*local tet + corner
+    __shared__ ushort4 s_inc[TILE_TETS];    // the tile's incidence list
 
     const int b = blockIdx.x;
     const int j = threadIdx.x;
@@ -54,6 +142,7 @@ __global__ void __launch_bounds__(TILE_TETS) k_tet_pass(MeshDev m, StateDev s, M
     const int nn = m.tile_node_begin[b + 1] - nb;
     const bool act = j < ntt;
     const int t = tb + j;
+    const bool wf = fields_due(s, fields_every, t_offset);
 
     // streaming per-tetra data first (read once per step: evict-first)
     uchar4 lc = make_uchar4(0, 0, 0, 0);
@@ -80,79 +169,225 @@ __global__ void __launch_bounds__(TILE_TETS) k_tet_pass(MeshDev m, StateDev s, M
         s_ul[j] = s.ul[node.x];
     }
     __syncthreads();
+    if (act) element_eval<MODEL>(j, t, lc, da, db, dc, pa, pb, pc, s_uh, s_ul, s_cf, s, mat, wf);
+    __syncthreads();
+    if (j < nn) node_flush(node, reinterpret_cast<const unsigned short*>(s_inc), s_cf, s, m.np);
+}
 
-    if (act) {
-        const int li[4] = {lc.x, lc.y, lc.z, lc.w};
-        const float4 u0h = s_uh[li[0]], u0l = s_ul[li[0]];
-        float d[3][3];
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-            const float4 h = s_uh[li[k + 1]], l = s_ul[li[k + 1]];
-            d[k][0] = (h.x - u0h.x) + (l.x - u0l.x);
-            d[k][1] = (h.y - u0h.y) + (l.y - u0l.y);
-            d[k][2] = (h.z - u0h.z) + (l.z - u0l.z);
-        }
-        const float Dmi[9] = {da.x, da.y, da.z, da.w, db.x, db.y, db.z, db.w, dc.x};
-        const float V0 = dc.y;
-        float f[4][3];
-        float jm1;
-        if (MODEL == MODEL_MR) {
-            jm1 = mr_element(d[0], d[1], d[2], Dmi, V0, mat.mu1, mat.mu2, mat.kappa, f);
-        } else if (MODEL == MODEL_SVK) {
-            jm1 = svk_element(d[0], d[1], d[2], Dmi, V0, mat.mu, mat.kp, f);
-        } else if (MODEL == MODEL_SVKK) {
-            jm1 = svkk_element(d[0], d[1], d[2], Dmi, V0, mat.mu, mat.kp, f);
-        } else {
-            VPParams par;
-            par.mu1 = mat.mu1;
-            par.mu2 = mat.mu2;
-            par.kappa = mat.kappa;
-            par.flow_exp = mat.flow_exp;
-            par.yield = mat.yield;
-            par.flow_rate = mat.flow_rate;
-            par.hard_thr = mat.hard_thr;
-            par.hard_exp = mat.hard_exp;
-            float P[9] = {pa.x, pa.y, pa.z, pa.w, pb.x, pb.y, pb.z, pb.w, pc.x};
-            float eps = pc.y;
-            float dP[9], rate, vm, pr;
-            vp_element(d[0], d[1], d[2], Dmi, V0, par, P, eps, dP, rate, f, vm, pr, jm1);
-#pragma unroll
-            for (int q = 0; q < 9; q++) P[q] += dP[q];
-            eps += rate;
-            __stcs(s.vp_a + t, make_float4(P[0], P[1], P[2], P[3]));
-            __stcs(s.vp_b + t, make_float4(P[4], P[5], P[6], P[7]));
-            __stcs(s.vp_c + t, make_float2(P[8], eps));
-            if (fields_every > 0) {
-                const long long tt = *s.time + t_offset;
-                if ((tt + 1) % fields_every == 0) __stcs(s.fields + t, make_float2(vm, pr));
-            }
-        }
-        if (!(jm1 > -1.0f)) atomicOr(s.status, STATUS_INVERTED);
-#pragma unroll
-        for (int k = 0; k < 4; k++) s_cf[4 * j + k] = make_float4(f[k][0], f[k][1], f[k][2], 0.f);
+// ------------------------------------------------------------------------------------------
+// Element pass, persistent and pipelined
+//
+// Each CTA walks the tiles blockIdx.x, blockIdx.x + gridDim.x, ... through two shared-memory
+// stages. One thread fills a stage with the tile's contiguous per-tetra streams and node list by
+// bulk asynchronous copies (cp.async.bulk, the TMA engine) that complete on the stage's
+// mbarrier; one tile ahead, all threads gather the tile's node displacements with cp.async.
+// While tile i is evaluated, tile i+1's node data and tile i+2's streams are in flight.
+// ------------------------------------------------------------------------------------------
+struct StageLayout {
+    // byte offsets inside one stage (all multiples of 16)
+    static constexpr unsigned LCONN = 0;                       // uchar4[256]
+    static constexpr unsigned DMI_A = LCONN + 4 * TILE_TETS;   // float4[256]
+    static constexpr unsigned DMI_B = DMI_A + 16 * TILE_TETS;  // float4[256]
+    static constexpr unsigned DMI_C = DMI_B + 16 * TILE_TETS;  // float2[256]
+    static constexpr unsigned INC = DMI_C + 8 * TILE_TETS;     // ushort4[256]
+    static constexpr unsigned NODES = INC + 8 * TILE_TETS;     // uint2[258]
+    static constexpr unsigned UH = NODES + 8 * (TILE_NODES_MAX + 2);
+    static constexpr unsigned UL = UH + 16 * TILE_NODES_MAX;
+    static constexpr unsigned VP_A = UL + 16 * TILE_NODES_MAX;
+    static constexpr unsigned VP_B = VP_A + 16 * TILE_TETS;
+    static constexpr unsigned VP_C = VP_B + 16 * TILE_TETS;
+    static constexpr unsigned SIZE_ELASTIC = VP_A;
+    static constexpr unsigned SIZE_VP = VP_C + 8 * TILE_TETS;
+};
+static_assert(StageLayout::UH % 16 == 0 && StageLayout::SIZE_VP % 16 == 0, "stage layout must be 16-byte aligned");
+
+constexpr unsigned PIPE_CF_BYTES = 16 * 4 * TILE_TETS;  // corner forces
+constexpr unsigned PIPE_HDR_BYTES = 64;                 // two mbarriers + two stage headers
+
+__host__ __device__ constexpr unsigned pipe_stage_bytes(int model) {
+    return model == MODEL_VP ? StageLayout::SIZE_VP : StageLayout::SIZE_ELASTIC;
+}
+__host__ __device__ constexpr unsigned pipe_smem_bytes(int model) {
+    return 2 * pipe_stage_bytes(model) + PIPE_CF_BYTES + PIPE_HDR_BYTES;
+}
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: gives up after MBAR_WAIT_LIMIT polls (each try_wait may itself suspend briefly).
+constexpr int MBAR_WAIT_LIMIT = 1 << 22;
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
+    for (int i = 0; i < MBAR_WAIT_LIMIT; i++)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ unsigned round16(unsigned b) { return (b + 15u) & ~15u; }
+
+struct StageHdr {
+    int tb, ntt, nn, noff;
+};
+
+// Thread 0: issue the bulk copies of `tile` into stage `st` (header written first; the
+// mbarrier's release/acquire makes it visible to the waiting threads).
+template <int MODEL>
+__device__ __forceinline__ void issue_tile(const MeshDev& m, const StateDev& s, int tile, unsigned char* st,
+                                           StageHdr* hdr, unsigned long long* bar) {
+    const int tb = m.tile_tet_begin[tile], ntt = m.tile_tet_begin[tile + 1] - tb;
+    const int nb = m.tile_node_begin[tile], nn = m.tile_node_begin[tile + 1] - nb;
+    const int nb0 = nb & ~1;          // 16-byte aligned start of the node list
+    const int noff = nb - nb0;
+    const unsigned nodes_b = round16(8u * (unsigned)(nn + noff));
+    const unsigned b4 = round16(4u * ntt), b8 = round16(8u * ntt), b16 = 16u * ntt;
+    unsigned total = b4 + 2 * b16 + 2 * b8 + nodes_b;
+    if (MODEL == MODEL_VP) total += 2 * b16 + b8;
+    hdr->tb = tb;
+    hdr->ntt = ntt;
+    hdr->nn = nn;
+    hdr->noff = noff;
+    mbar_arrive_expect_tx(bar, total);
+    bulk_load(st + StageLayout::LCONN, m.lconn + tb, b4, bar);
+    bulk_load(st + StageLayout::DMI_A, m.dmi_a + tb, b16, bar);
+    bulk_load(st + StageLayout::DMI_B, m.dmi_b + tb, b16, bar);
+    bulk_load(st + StageLayout::DMI_C, m.dmi_c + tb, b8, bar);
+    bulk_load(st + StageLayout::INC, m.tile_inc + tb, b8, bar);
+    bulk_load(st + StageLayout::NODES, m.tile_nodes + nb0, nodes_b, bar);
+    if (MODEL == MODEL_VP) {
+        bulk_load(st + StageLayout::VP_A, s.vp_a + tb, b16, bar);
+        bulk_load(st + StageLayout::VP_B, s.vp_b + tb, b16, bar);
+        bulk_load(st + StageLayout::VP_C, s.vp_c + tb, b8, bar);
+    }
+}
+
+// All threads: gather the node displacements of the tile in stage `st` (cp.async, one group).
+__device__ __forceinline__ void gather_nodes(const StateDev& s, unsigned char* st, const StageHdr& h) {
+    const uint2* nodes = reinterpret_cast<const uint2*>(st + StageLayout::NODES) + h.noff;
+    float4* uh = reinterpret_cast<float4*>(st + StageLayout::UH);
+    float4* ul = reinterpret_cast<float4*>(st + StageLayout::UL);
+    for (int j = threadIdx.x; j < h.nn; j += TILE_TETS) {
+        const unsigned g = nodes[j].x;
+        cp_async16(uh + j, s.uh + g);
+        cp_async16(ul + j, s.ul + g);
+    }
+    cp_async_commit();
+}
+
+template <int MODEL>
+__global__ void __launch_bounds__(TILE_TETS) k_tet_pass_pipe(MeshDev m, StateDev s, MaterialDev mat,
+                                                             long long fields_every, int t_offset) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    constexpr unsigned SB = pipe_stage_bytes(MODEL);
+    unsigned char* stage[2] = {smem, smem + SB};
+    float4* s_cf = reinterpret_cast<float4*>(smem + 2 * SB);
+    unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem + 2 * SB + PIPE_CF_BYTES);
+    StageHdr* hdr = reinterpret_cast<StageHdr*>(smem + 2 * SB + PIPE_CF_BYTES + 16);
+    __shared__ int s_ok;
+
+    const int j = threadIdx.x;
+    const int G = gridDim.x;
+    const int first = blockIdx.x;
+    const bool wf = fields_due(s, fields_every, t_offset);
+    if (first >= m.ntiles) return;
+
+    if (j == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        issue_tile<MODEL>(m, s, first, stage[0], &hdr[0], &bar[0]);
+        if (first + G < m.ntiles) issue_tile<MODEL>(m, s, first + G, stage[1], &hdr[1], &bar[1]);
+        s_ok = mbar_wait_bounded(&bar[0], 0);
     }
     __syncthreads();
-    // Each tile node sums its corner forces in the tile's fixed incidence order, then adds the
-    // sum to the global accumulator as 64-bit fixed point: the total is independent of the
-    // order in which tiles finish.
-    if (j < nn) {
-        const unsigned first = node.y >> 16, count = node.y & 0xffffu;
-        const unsigned short* inc = reinterpret_cast<const unsigned short*>(s_inc);
-        float fx = 0.f, fy = 0.f, fz = 0.f;
-        for (unsigned q = 0; q < count; q++) {
-            const float4 c = s_cf[inc[first + q]];
-            fx += c.x;
-            fy += c.y;
-            fz += c.z;
-        }
-        if (!(fabsf(fx) <= FORCE_FIX_MAX && fabsf(fy) <= FORCE_FIX_MAX && fabsf(fz) <= FORCE_FIX_MAX)) {
-            atomicOr(s.status, STATUS_NONFINITE);
+    bool ok = s_ok != 0;
+    if (ok) gather_nodes(s, stage[0], hdr[0]);
+
+    for (int it = 0; ok; it++) {
+        const int tile = first + it * G;
+        if (tile >= m.ntiles) break;
+        const int cur = it & 1, nxt = cur ^ 1;
+        const bool has_next = tile + G < m.ntiles;
+        // tile it+1: wait for its streams, start gathering its nodes
+        if (has_next) {
+            if (j == 0) s_ok = mbar_wait_bounded(&bar[nxt], (unsigned)((it + 1) >> 1) & 1u);
+            __syncthreads();
+            if (!s_ok) {
+                ok = false;
+                break;
+            }
+            gather_nodes(s, stage[nxt], hdr[nxt]);
+            cp_async_wait<1>();
         } else {
-            const long long np = m.np;
-            atomicAdd(s.facc + node.x, (unsigned long long)__float2ll_rn(fx * FORCE_FIX_SCALE));
-            atomicAdd(s.facc + np + node.x, (unsigned long long)__float2ll_rn(fy * FORCE_FIX_SCALE));
-            atomicAdd(s.facc + 2 * np + node.x, (unsigned long long)__float2ll_rn(fz * FORCE_FIX_SCALE));
+            cp_async_wait<0>();
         }
+        __syncthreads();  // tile it: streams and node data visible to all threads
+
+        const StageHdr h = hdr[cur];
+        unsigned char* st = stage[cur];
+        if (j < h.ntt) {
+            const float4* vpa = reinterpret_cast<const float4*>(st + StageLayout::VP_A);
+            const float4* vpb = reinterpret_cast<const float4*>(st + StageLayout::VP_B);
+            const float2* vpc = reinterpret_cast<const float2*>(st + StageLayout::VP_C);
+            float4 pa = make_float4(0.f, 0.f, 0.f, 0.f), pb = pa;
+            float2 pc = make_float2(0.f, 0.f);
+            if (MODEL == MODEL_VP) {
+                pa = vpa[j];
+                pb = vpb[j];
+                pc = vpc[j];
+            }
+            element_eval<MODEL>(j, (long long)h.tb + j, reinterpret_cast<const uchar4*>(st + StageLayout::LCONN)[j],
+                                reinterpret_cast<const float4*>(st + StageLayout::DMI_A)[j],
+                                reinterpret_cast<const float4*>(st + StageLayout::DMI_B)[j],
+                                reinterpret_cast<const float2*>(st + StageLayout::DMI_C)[j], pa, pb, pc,
+                                reinterpret_cast<const float4*>(st + StageLayout::UH),
+                                reinterpret_cast<const float4*>(st + StageLayout::UL), s_cf, s, mat, wf);
+        }
+        __syncthreads();  // corner forces complete
+        if (j < h.nn) {
+            const uint2 node = reinterpret_cast<const uint2*>(st + StageLayout::NODES)[h.noff + j];
+            node_flush(node, reinterpret_cast<const unsigned short*>(st + StageLayout::INC), s_cf, s, m.np);
+        }
+        __syncthreads();  // stage `cur` and the corner forces are free again
+        if (j == 0 && tile + 2 * G < m.ntiles) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue_tile<MODEL>(m, s, tile + 2 * G, stage[cur], &hdr[cur], &bar[cur]);
+        }
+    }
+    cp_async_wait<0>();
+    if (!ok && j == 0) {
+        atomicOr(s.status, STATUS_TIMEOUT);
+        // let copies still in flight land before the CTA's shared memory is released
+        mbar_wait_bounded(&bar[0], 0);
+        mbar_wait_bounded(&bar[1], 0);
     }
 }
 
@@ -362,6 +597,48 @@ __global__ void k_vec_from_user(int np, float4* a, const long long* node_user, c
 // ------------------------------------------------------------------------------------------
 // Launchers
 // ------------------------------------------------------------------------------------------
+template <int MODEL>
+static cudaError_t launch_pipe(const MeshDev& m, const StateDev& s, const MaterialDev& mat, const StepParams& p,
+                               int t_offset, int grid, cudaStream_t st) {
+    const unsigned bytes = pipe_smem_bytes(MODEL);
+    static bool attr_set = false;  // per process; the attribute is per function
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(k_tet_pass_pipe<MODEL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)bytes);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    k_tet_pass_pipe<MODEL><<<grid, TILE_TETS, bytes, st>>>(m, s, mat, p.fields_every, t_offset);
+    return cudaGetLastError();
+}
+
+int pipe_blocks_per_sm(int model) {
+    int n = 0;
+    cudaError_t e = cudaSuccess;
+    auto q = [&](auto kern, unsigned bytes) {
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, TILE_TETS, bytes);
+    };
+    switch (model) {
+        case MODEL_MR: q(k_tet_pass_pipe<MODEL_MR>, pipe_smem_bytes(MODEL_MR)); break;
+        case MODEL_SVK: q(k_tet_pass_pipe<MODEL_SVK>, pipe_smem_bytes(MODEL_SVK)); break;
+        case MODEL_SVKK: q(k_tet_pass_pipe<MODEL_SVKK>, pipe_smem_bytes(MODEL_SVKK)); break;
+        default: q(k_tet_pass_pipe<MODEL_VP>, pipe_smem_bytes(MODEL_VP)); break;
+    }
+    return e == cudaSuccess ? n : 0;
+}
+
+cudaError_t launch_tet_pass_pipe(const MeshDev& m, const StateDev& s, const MaterialDev& mat, const StepParams& p,
+                                 int t_offset, int grid, cudaStream_t st) {
+    switch (mat.model) {
+        case MODEL_MR: return launch_pipe<MODEL_MR>(m, s, mat, p, t_offset, grid, st);
+        case MODEL_SVK: return launch_pipe<MODEL_SVK>(m, s, mat, p, t_offset, grid, st);
+        case MODEL_SVKK: return launch_pipe<MODEL_SVKK>(m, s, mat, p, t_offset, grid, st);
+        case MODEL_VP: return launch_pipe<MODEL_VP>(m, s, mat, p, t_offset, grid, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
 cudaError_t launch_tet_pass(const MeshDev& m, const StateDev& s, const MaterialDev& mat, const StepParams& p,
                             int t_offset, cudaStream_t st) {
     const dim3 grid((unsigned)m.ntiles), block(TILE_TETS);

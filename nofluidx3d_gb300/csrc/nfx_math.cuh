@@ -33,10 +33,20 @@ NFX_HD float rcbrt_(float x) {
 }
 NFX_HD float pow_(float x, float y) { return powf(x, y); }
 NFX_HD float sqrt_(float x) { return sqrtf(x); }
+// a / b to within 2 ulp (the reciprocal-based divide), used where FP32 rounding of the quotient
+// is far below the scheme's other errors.
+NFX_HD float fdiv_(float a, float b) {
+#if defined(__CUDA_ARCH__)
+    return __fdividef(a, b);
+#else
+    return a / b;
+#endif
+}
 #else
 NFX_HD float rcbrt_(float x) { return 1.0f / std::cbrt(x); }
 NFX_HD float pow_(float x, float y) { return std::pow(x, y); }
 NFX_HD float sqrt_(float x) { return std::sqrt(x); }
+NFX_HD float fdiv_(float a, float b) { return a / b; }
 #endif
 
 // Symmetric 3x3 stored as (xx, yy, zz, xy, yz, xz).
@@ -307,37 +317,29 @@ struct VPParams {
 // Multiplicative finite-strain viscoplastic element,
 // InteractionFiniteStrainViscoplastic.cl:30-206. The plastic deformation tensor is carried as
 // its deviation from the identity, P = Fp - I, so that FP32 resolves the small per-step
-// increments Fp += Fe^-1 Dp F (:171-206). Fe = F Fp^-1 (:59-79), Be = Fe Fe^T (:82-84),
-// J = sqrt(det Be) = |det Fe| (:87), sigma of the Mooney-Rivlin law (:105-107), nodal forces
-// one third of the adjacent face tractions (:110-141), which for a linear tetrahedron equal
-// -|V| sigma grad N_i, i.e. rows of -V0 sign(det F) Dm^-1 adj(F) sigma.
-// Reads P (9); writes its increment dP = Fe^-1 Dp F (9) and the plastic strain rate, which the
-// caller adds to its stored state; writes von Mises and pressure.
+// increments Fp += Fe^-1 Dp F (:171-206). Mathematically identical forms with fewer operations:
+//   Fe - I = F Fp^-1 - I = (F - Fp) Fp^-1 = (H - P) adj(I + P) / det(I + P)      (:59-79)
+//   Fe^-1 Dp F = Fp F^-1 Dp F = (I + P) M,   M = adj(F) Dp F / det F               (:171-195)
+// Be = Fe Fe^T (:82-84), J = sqrt(det Be) = |det Fe| (:87), sigma of the Mooney-Rivlin law
+// (:105-107), nodal forces one third of the adjacent face tractions (:110-141), which for a
+// linear tetrahedron equal -|V| sigma grad N_i, i.e. rows of -V0 sign(det F) Dm^-1 adj(F) sigma.
+// Reads P (9); writes its increment dP (9) and the plastic strain rate, which the caller adds
+// to its stored state; writes von Mises and pressure.
 NFX_HD void vp_element(const float d1[3], const float d2[3], const float d3[3], const float* Dmi, float V0,
                        const VPParams& par, const float Pp[9], float eps, float dP[9], float& rate_out,
                        float f[4][3], float& vm_out, float& p_out, float& Jm1_out) {
     const Mat3 H = disp_grad(d1, d2, d3, Dmi);
-    // Fp^-1 = adj(I + P) / det(I + P)
     Mat3 Pm;
 #pragma unroll
     for (int k = 0; k < 9; k++) Pm.m[k] = Pp[k];
     const Mat3 adjFp = adj_1p(Pm);
-    // G = Fe - I = [adj(I+P) - det(I+P) I + H adj(I+P)] / det(I+P), where
-    // adj(I+P) - det(I+P) I = -(1 + tr P) P + P^2 - det(P) I holds only small terms.
-    const float p = Pm.m[0] + Pm.m[4] + Pm.m[8];
-    const float* q = Pm.m;
-    const float detP = q[0] * (q[4] * q[8] - q[5] * q[7]) - q[1] * (q[3] * q[8] - q[5] * q[6]) +
-                       q[2] * (q[3] * q[7] - q[4] * q[6]);
-    const float detFp = 1.0f + det1p_minus1(Pm);
-    const float rdet = 1.0f / detFp;
-    const Mat3 P2 = mul3(Pm, Pm);
-    const Mat3 HA = mul3(H, adjFp);
-    Mat3 G;
+    const float rdet = fdiv_(1.0f, 1.0f + det1p_minus1(Pm));
+    Mat3 D;
 #pragma unroll
-    for (int k = 0; k < 9; k++) G.m[k] = (HA.m[k] + (P2.m[k] - (1.0f + p) * q[k])) * rdet;
-    G.m[0] -= detP * rdet;
-    G.m[4] -= detP * rdet;
-    G.m[8] -= detP * rdet;
+    for (int k = 0; k < 9; k++) D.m[k] = H.m[k] - Pm.m[k];
+    Mat3 G = mul3(D, adjFp);
+#pragma unroll
+    for (int k = 0; k < 9; k++) G.m[k] *= rdet;
     // elastic left strain and volume change
     const Sym3 Ee = left_strain(G);
     const float JeM1 = det1p_minus1(G);  // det Fe - 1
@@ -359,30 +361,39 @@ NFX_HD void vp_element(const float d1[3], const float d2[3], const float d3[3], 
     const float sigma0 = par.yield * (par.hard_exp == 0.0f ? 1.0f : pow_(1.0f + eps / par.hard_thr, par.hard_exp));
     vm_out = vm;
     p_out = t3;
-    const float ratio = vm / sigma0;
+    const float ratio = fdiv_(vm, sigma0);
     const float rate = par.flow_rate * (par.flow_exp == 1.0f ? ratio : pow_(ratio, par.flow_exp));
     rate_out = rate;
 #pragma unroll
     for (int q = 0; q < 9; q++) dP[q] = 0.0f;
     if (vm != 0.0f) {
-        const float k = rate * 1.5f / vm;
-        const Mat3 Dp = {{dxx * k, s.xy * k, s.xz * k, s.xy * k, dyy * k, s.yz * k, s.xz * k, s.yz * k, dzz * k}};
-        // Fe^-1 = Fp F^-1 = (I + P) adj(I + H) / det(I + H)
-        Mat3 IP = Pm;
-        IP.m[0] += 1.0f;
-        IP.m[4] += 1.0f;
-        IP.m[8] += 1.0f;
-        const float rJ = 1.0f / (1.0f + JFm1);
-        Mat3 Fei = mul3(IP, A);
+        const float k = fdiv_(rate * 1.5f, vm);
+        const float Dp[9] = {dxx * k, s.xy * k, s.xz * k, s.xy * k, dyy * k, s.yz * k, s.xz * k, s.yz * k, dzz * k};
+        // T = adj(F) Dp, then M = T (I + H) / det F
+        float T[9];
 #pragma unroll
-        for (int q = 0; q < 9; q++) Fei.m[q] *= rJ;
-        Mat3 F = H;
-        F.m[0] += 1.0f;
-        F.m[4] += 1.0f;
-        F.m[8] += 1.0f;
-        const Mat3 dFp = mul3(mul3(Fei, Dp), F);
+        for (int i = 0; i < 3; i++) {
 #pragma unroll
-        for (int q = 0; q < 9; q++) dP[q] = dFp.m[q];
+            for (int j = 0; j < 3; j++)
+                T[3 * i + j] = A.m[3 * i] * Dp[j] + A.m[3 * i + 1] * Dp[3 + j] + A.m[3 * i + 2] * Dp[6 + j];
+        }
+        const float rJ = fdiv_(1.0f, 1.0f + JFm1);
+        float M[9];
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+#pragma unroll
+            for (int j = 0; j < 3; j++)
+                M[3 * i + j] = (T[3 * i + j] + (T[3 * i] * H.m[j] + T[3 * i + 1] * H.m[3 + j] +
+                                                T[3 * i + 2] * H.m[6 + j])) * rJ;
+        }
+        // dP = (I + P) M
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+#pragma unroll
+            for (int j = 0; j < 3; j++)
+                dP[3 * i + j] = M[3 * i + j] + (Pm.m[3 * i] * M[j] + Pm.m[3 * i + 1] * M[3 + j] +
+                                                Pm.m[3 * i + 2] * M[6 + j]);
+        }
     }
 }
 

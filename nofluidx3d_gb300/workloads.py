@@ -129,7 +129,7 @@ def plain_large_1m() -> Workload:
 
 
 def plain_large_r48() -> Workload:
-    """The same construction at R = 48 (2,778,816 tetra): large enough that one step's
+    """The same construction at R = 48 (2,780,400 tetra): large enough that one step's
     viscoplastic state (~350 MB read + written) exceeds L2, small enough for full ncu captures."""
     return plain_large().with_(name="plain-large R48 MR+VP sphere", radius=48.0)
 

@@ -119,6 +119,23 @@ def test_gpu_graph_chunks_match_single_steps():
     b.close()
 
 
+@pytest.mark.parametrize("name", ["nh_plane_R3", "vp_sphere_R3"])
+def test_gpu_bitwise_reproducible(name):
+    """Nodal forces accumulate as fixed-point integers and every reduction has a fixed order,
+    so two runs of the same case agree to the bit."""
+    w = CASES[name].workload
+    runs = []
+    for _ in range(2):
+        sim = CellSim(0)
+        w.configure(sim)
+        sim.step(257)
+        sim.record_now()
+        runs.append((sim.points(), sim.velocities(), sim.curve(), sim.plastic_tensor_soa()))
+        sim.close()
+    for a, b in zip(*runs):
+        assert np.array_equal(a, b)
+
+
 def test_gpu_indenter_force_equals_recorded_row():
     w = CASES["nh_plane_R3"].workload
     sim = CellSim(0)
