@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -69,7 +70,8 @@ struct nfx_sim {
     cudaGraphExec_t graph = nullptr;
     bool graph_valid = false;
     int sm_count = 1;
-    int tet_variant = 1;                   // 1: persistent pipelined element pass, 0: one CTA per tile
+    int tet_variant = 0;                   // 1: persistent pipelined element pass, 0: one CTA per tile
+    int tile_tets = TILE_TETS;             // tetrahedra per tile (128, 256 or 512)
     int pipe_bps[4] = {-1, -1, -1, -1};    // resident CTAs per SM of the pipelined kernel, per model
 };
 
@@ -119,11 +121,11 @@ int require_ready(nfx_sim* s) {
     return NFX_OK;
 }
 
-// Element pass launch: the persistent pipelined kernel on a grid of (resident CTAs per SM) x
-// (SM count), capped at the tile count; the one-CTA-per-tile kernel when selected
-// (NFX_TET_KERNEL=0 in the environment) or when the pipelined kernel cannot be resident.
+// Element pass launch: the one-CTA-per-tile kernel by default. NFX_TET_KERNEL=1 in the
+// environment selects the persistent pipelined kernel (256-tetra tiles only) on a grid of
+// (resident CTAs per SM) x (SM count), capped at the tile count.
 cudaError_t launch_elem(nfx_sim* s, int k) {
-    if (s->tet_variant == 1) {
+    if (s->tet_variant == 1 && s->mesh.tile_tets == TILE_TETS) {
         int& bps = s->pipe_bps[s->mat.model & 3];
         if (bps < 0) bps = pipe_blocks_per_sm(s->mat.model);
         if (bps > 0) {
@@ -213,7 +215,11 @@ int nfx_create(int device, nfx_sim** out) {
     s->prm.fix_a = s->prm.fix_b = -1;
     cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, device);
     if (s->sm_count < 1) s->sm_count = 1;
-    if (const char* v = std::getenv("NFX_TET_KERNEL")) s->tet_variant = std::atoi(v) == 0 ? 0 : 1;
+    if (const char* v = std::getenv("NFX_TET_KERNEL")) s->tet_variant = std::atoi(v) == 1 ? 1 : 0;
+    if (const char* v = std::getenv("NFX_TILE_TETS")) {
+        const int t = std::atoi(v);
+        if (t == 128 || t == 256 || t == 512) s->tile_tets = t;
+    }
     // default integrator: the reference's xi = 0.005 (VelocityVerlet.cl:11)
     const double xi = 0.005;
     s->prm.vv_a = (float)((1 - 0.5 * xi) / (1 + 0.5 * xi));
@@ -250,7 +256,7 @@ int nfx_set_mesh(nfx_sim* s, int64_t np, int64_t nt, const double* points, const
     if ((rc = set_device(s)) != NFX_OK) return rc;
     MeshPlan plan;
     std::string err;
-    if (!build_mesh_plan(np, nt, points, tets, plan, err)) return fail(NFX_ERR_ARG, err);
+    if (!build_mesh_plan(np, nt, points, tets, s->tile_tets, plan, err)) return fail(NFX_ERR_ARG, err);
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     invalidate_graph(s);
     free_mesh(s);
@@ -308,6 +314,7 @@ int nfx_set_mesh(nfx_sim* s, int64_t np, int64_t nt, const double* points, const
     s->mesh.np = (int)np;
     s->mesh.nt = (int)nt;
     s->mesh.ntiles = (int)P.ntiles;
+    s->mesh.tile_tets = P.tile_tets;
     s->mesh.tile_tet_begin = tb;
     s->mesh.tile_node_begin = nbg;
     s->mesh.tile_nodes = tn;

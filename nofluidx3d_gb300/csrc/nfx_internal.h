@@ -16,8 +16,10 @@ constexpr int MAX_CONTACTS = 4;
 // A tile is a run of consecutive tetrahedra (after reordering) processed by one CTA. Its
 // distinct nodes are listed once, so the per-tetra connectivity is four 8-bit local indices
 // and the tile's nodal forces are summed in shared memory before one flush per node.
-constexpr int TILE_TETS = 256;
-constexpr int TILE_NODES_MAX = 256;
+constexpr int TILE_TETS = 256;       // default tile size (the pipelined kernel's only size)
+constexpr int TILE_NODES_MAX = 256;  // 8-bit local corner indices
+// Tile sizes the one-CTA-per-tile kernel is built for; a tile has at most min(tile, 256) nodes.
+constexpr int TILE_SIZES[3] = {128, 256, 512};
 constexpr int NODE_BLOCK = 256;
 
 // Fixed-point scale of the force accumulator: 2^40 (resolution 9.1e-13, range +-8.4e6).
@@ -40,6 +42,7 @@ constexpr int ARRAY_PAD = 16;
 // ---------------------------------------------------------------------------------------
 struct MeshPlan {
     int64_t np = 0, nt = 0, ntiles = 0;
+    int tile_tets = TILE_TETS;
     std::vector<int64_t> node_user;   // internal node -> user node id
     std::vector<int64_t> node_int;    // user node id -> internal node
     std::vector<int64_t> tet_user;    // internal tetra -> user tetra id
@@ -56,14 +59,15 @@ struct MeshPlan {
 
 // Builds the plan from the reference's layouts (points SoA 3*np doubles, tets SoA 4*nt).
 // Returns false with a message on invalid input (index out of range, degenerate tetra).
-bool build_mesh_plan(int64_t np, int64_t nt, const double* points_soa, const uint32_t* tets_soa, MeshPlan& plan,
-                     std::string& err);
+bool build_mesh_plan(int64_t np, int64_t nt, const double* points_soa, const uint32_t* tets_soa, int tile_tets,
+                     MeshPlan& plan, std::string& err);
 
 // ---------------------------------------------------------------------------------------
 // Device views passed to kernels by value.
 // ---------------------------------------------------------------------------------------
 struct MeshDev {
     int np, nt, ntiles;
+    int tile_tets;
     const int* tile_tet_begin;
     const int* tile_node_begin;
     const uint2* tile_nodes;   // (node id, first << 16 | count)

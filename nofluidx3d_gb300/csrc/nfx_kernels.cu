@@ -126,13 +126,13 @@ __device__ __forceinline__ bool fields_due(const StateDev& s, long long fields_e
 // ------------------------------------------------------------------------------------------
 // Element pass, one CTA per tile (plain loads)
 // ------------------------------------------------------------------------------------------
-template <int MODEL>
-__global__ void __launch_bounds__(TILE_TETS) k_tet_pass(MeshDev m, StateDev s, MaterialDev mat,
-                                                        long long fields_every, int t_offset) {
+template <int MODEL, int TILE>
+__global__ void __launch_bounds__(TILE) k_tet_pass(MeshDev m, StateDev s, MaterialDev mat, long long fields_every,
+                                                   int t_offset) {
     __shared__ float4 s_uh[TILE_NODES_MAX];
     __shared__ float4 s_ul[TILE_NODES_MAX];
-    __shared__ float4 s_cf[4 * TILE_TETS];  // corner forces, slot 4*local tet + corner
-    __shared__ ushort4 s_inc[TILE_TETS];    // the tile's incidence list
+    __shared__ float4 s_cf[4 * TILE];  // corner forces, slot 4*local tet + corner
+    __shared__ ushort4 s_inc[TILE];    // the tile's incidence list
 
     const int b = blockIdx.x;
     const int j = threadIdx.x;
@@ -444,13 +444,15 @@ __device__ void grid_sum_finish(const StateDev& s, double val, bool to_scalar, l
 }
 
 // Contact force on one node in double precision (the reference's FP64 formulas). Returns the
-// y component for the readout; adds the force to f.
-__device__ __forceinline__ double contact_force(const ContactDev& c, double w, const float4& xh, const float4& xl,
+// y component for the readout; adds the force to f. The low part of the reference position is
+// only read for nodes that pass the coarse test.
+__device__ __forceinline__ double contact_force(const ContactDev& c, double w, const float4& xh, const float4* xlp,
                                                 const float4& uh, const float4& ul, float4& f) {
     // coarse test in float: nodes farther than 1e-3 from contact cannot touch
     const float yf = xh.y + uh.y;
     if (c.kind == CONTACT_SUBSTRATE) {
         if ((float)w - yf < -1e-3f) return 0.0;
+        const float4 xl = *xlp;
         const double y = ((double)xh.y + (double)xl.y) + ((double)uh.y + (double)ul.y);
         const double dis = fmax(w - y, 0.0);
         const double fy = c.k * dis;
@@ -459,6 +461,7 @@ __device__ __forceinline__ double contact_force(const ContactDev& c, double w, c
     }
     if (c.kind == CONTACT_PLANE) {
         if (yf - (float)w < -1e-3f) return 0.0;
+        const float4 xl = *xlp;
         const double y = ((double)xh.y + (double)xl.y) + ((double)uh.y + (double)ul.y);
         const double dis = fmax(y - w, 0.0);
         const double fy = -c.k * dis;
@@ -469,6 +472,7 @@ __device__ __forceinline__ double contact_force(const ContactDev& c, double w, c
     const float rxf = xh.x + uh.x, ryf = yf - (float)w, rzf = xh.z + uh.z;
     const float rr = (float)c.radius + 1e-3f;
     if (rxf * rxf + ryf * ryf + rzf * rzf > rr * rr) return 0.0;
+    const float4 xl = *xlp;
     const double rx = ((double)xh.x + (double)xl.x) + ((double)uh.x + (double)ul.x);
     const double ry = (((double)xh.y + (double)xl.y) + ((double)uh.y + (double)ul.y)) - w;
     const double rz = ((double)xh.z + (double)xl.z) + ((double)uh.z + (double)ul.z);
@@ -510,11 +514,11 @@ __global__ void __launch_bounds__(NODE_BLOCK) k_node_pass(MeshDev m, StateDev s,
         float4 f = make_float4(__ll2float_rn((long long)s.facc[i]) * FORCE_FIX_INV,
                                __ll2float_rn((long long)s.facc[np + i]) * FORCE_FIX_INV,
                                __ll2float_rn((long long)s.facc[2 * np + i]) * FORCE_FIX_INV, 0.f);
-        const float4 xh = m.Xh[i], xl = m.Xl[i];
+        const float4 xh = m.Xh[i];
         float4 uh = s.uh[i], ul = s.ul[i];
         for (int c = 0; c < p.n_contacts; c++) {
             const double w = contact_pos(p.c[c], t);
-            const double fy = contact_force(p.c[c], w, xh, xl, uh, ul, f);
+            const double fy = contact_force(p.c[c], w, xh, m.Xl + i, uh, ul, f);
             if (c == rc) ro = -fy;
         }
         if (mode == NODE_UPDATE) {
@@ -527,6 +531,7 @@ __global__ void __launch_bounds__(NODE_BLOCK) k_node_pass(MeshDev m, StateDev s,
             df_add(uh.y, ul.y, p.vv_dm * v.y + 0.5f * f.y);
             df_add(uh.z, ul.z, p.vv_dm * v.z + 0.5f * f.z);
             if (i == p.fix_a || i == p.fix_b) {  // VelocityVerlet.cl:17-22: x = z = 0
+                const float4 xl = m.Xl[i];
                 uh.x = -xh.x;
                 ul.x = -xl.x;
                 uh.z = -xh.z;
@@ -639,17 +644,28 @@ cudaError_t launch_tet_pass_pipe(const MeshDev& m, const StateDev& s, const Mate
     }
 }
 
-cudaError_t launch_tet_pass(const MeshDev& m, const StateDev& s, const MaterialDev& mat, const StepParams& p,
-                            int t_offset, cudaStream_t st) {
-    const dim3 grid((unsigned)m.ntiles), block(TILE_TETS);
+template <int TILE>
+static cudaError_t launch_tile(const MeshDev& m, const StateDev& s, const MaterialDev& mat, const StepParams& p,
+                               int t_offset, cudaStream_t st) {
+    const dim3 grid((unsigned)m.ntiles), block(TILE);
     switch (mat.model) {
-        case MODEL_MR: k_tet_pass<MODEL_MR><<<grid, block, 0, st>>>(m, s, mat, p.fields_every, t_offset); break;
-        case MODEL_SVK: k_tet_pass<MODEL_SVK><<<grid, block, 0, st>>>(m, s, mat, p.fields_every, t_offset); break;
-        case MODEL_SVKK: k_tet_pass<MODEL_SVKK><<<grid, block, 0, st>>>(m, s, mat, p.fields_every, t_offset); break;
-        case MODEL_VP: k_tet_pass<MODEL_VP><<<grid, block, 0, st>>>(m, s, mat, p.fields_every, t_offset); break;
+        case MODEL_MR: k_tet_pass<MODEL_MR, TILE><<<grid, block, 0, st>>>(m, s, mat, p.fields_every, t_offset); break;
+        case MODEL_SVK: k_tet_pass<MODEL_SVK, TILE><<<grid, block, 0, st>>>(m, s, mat, p.fields_every, t_offset); break;
+        case MODEL_SVKK: k_tet_pass<MODEL_SVKK, TILE><<<grid, block, 0, st>>>(m, s, mat, p.fields_every, t_offset); break;
+        case MODEL_VP: k_tet_pass<MODEL_VP, TILE><<<grid, block, 0, st>>>(m, s, mat, p.fields_every, t_offset); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
+}
+
+cudaError_t launch_tet_pass(const MeshDev& m, const StateDev& s, const MaterialDev& mat, const StepParams& p,
+                            int t_offset, cudaStream_t st) {
+    switch (m.tile_tets) {
+        case 128: return launch_tile<128>(m, s, mat, p, t_offset, st);
+        case 256: return launch_tile<256>(m, s, mat, p, t_offset, st);
+        case 512: return launch_tile<512>(m, s, mat, p, t_offset, st);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 cudaError_t launch_node_pass(const MeshDev& m, const StateDev& s, const StepParams& p, int t_offset, int mode,

@@ -5,9 +5,10 @@
 //  * nodes are sorted along a Morton (Z-order) curve of their reference positions, and tetrahedra
 //    along the Morton curve of their centroids, so a run of consecutive tetrahedra touches a
 //    compact set of nodes;
-//  * consecutive tetrahedra are grouped into tiles of at most TILE_TETS elements and
-//    TILE_NODES_MAX distinct nodes, each tetra's corners stored as 8-bit indices into its
-//    tile's node list;
+//  * consecutive tetrahedra are grouped into tiles of at most tile_tets (128, 256 or 512)
+//    elements and min(tile_tets, 256) distinct nodes, each tetra's corners stored as 8-bit
+//    indices into its tile's node list, plus the tile's incidence list (corners grouped by
+//    node) for the fixed-order force sums;
 //  * Dm^-1 (inverse of the reference edge matrix [X1-X0, X2-X0, X3-X0]) and the signed
 //    reference volume V0 = det(Dm)/6 (TetraCell.py:33-41) are computed in double and stored
 //    as float;
@@ -50,7 +51,12 @@ struct Quant {
 
 }  // namespace
 
-bool build_mesh_plan(int64_t np, int64_t nt, const double* P, const uint32_t* T, MeshPlan& plan, std::string& err) {
+bool build_mesh_plan(int64_t np, int64_t nt, const double* P, const uint32_t* T, int tile_tets, MeshPlan& plan,
+                     std::string& err) {
+    if (tile_tets != 128 && tile_tets != 256 && tile_tets != 512) {
+        err = "tile size must be 128, 256 or 512";
+        return false;
+    }
     if (np <= 0 || nt <= 0) {
         err = "mesh needs at least one node and one tetra";
         return false;
@@ -74,6 +80,8 @@ bool build_mesh_plan(int64_t np, int64_t nt, const double* P, const uint32_t* T,
     plan = MeshPlan();
     plan.np = np;
     plan.nt = nt;
+    plan.tile_tets = tile_tets;
+    const int64_t nodes_max = std::min<int64_t>(TILE_NODES_MAX, tile_tets);
 
     // quantisation: cell size ~ mean node spacing
     Quant Q;
@@ -124,10 +132,10 @@ bool build_mesh_plan(int64_t np, int64_t nt, const double* P, const uint32_t* T,
     plan.tile_tet_begin.push_back(0);
     plan.tile_node_begin.push_back(0);
     std::vector<uint32_t> ids;
-    ids.reserve(4 * TILE_TETS);
+    ids.reserve(4 * (size_t)tile_tets);
     int64_t t0 = 0;
     while (t0 < nt) {
-        int64_t cnt = std::min<int64_t>(TILE_TETS, nt - t0);
+        int64_t cnt = std::min<int64_t>(tile_tets, nt - t0);
         for (;;) {
             ids.clear();
             for (int64_t j = 0; j < cnt; j++) {
@@ -136,7 +144,7 @@ bool build_mesh_plan(int64_t np, int64_t nt, const double* P, const uint32_t* T,
             }
             std::sort(ids.begin(), ids.end());
             ids.erase(std::unique(ids.begin(), ids.end()), ids.end());
-            if ((int64_t)ids.size() <= TILE_NODES_MAX || cnt == 1) break;
+            if ((int64_t)ids.size() <= nodes_max || cnt == 1) break;
             cnt = std::max<int64_t>(1, cnt - 16);
         }
         const size_t nn = ids.size();
