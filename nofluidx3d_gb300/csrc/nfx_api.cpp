@@ -71,7 +71,7 @@ struct nfx_sim {
     bool graph_valid = false;
     int sm_count = 1;
     int tet_variant = 0;                   // 1: persistent pipelined element pass, 0: one CTA per tile
-    int tile_tets = TILE_TETS;             // tetrahedra per tile (128, 256 or 512)
+    int tile_tets = TILE_TETS;             // tetrahedra per tile (64, 128, 256 or 512)
     int pipe_bps[4] = {-1, -1, -1, -1};    // resident CTAs per SM of the pipelined kernel, per model
 };
 
@@ -122,12 +122,12 @@ int require_ready(nfx_sim* s) {
 }
 
 // Element pass launch: the one-CTA-per-tile kernel by default. NFX_TET_KERNEL=1 in the
-// environment selects the persistent pipelined kernel (256-tetra tiles only) on a grid of
+// environment selects the persistent pipelined kernel (tiles of at most 256) on a grid of
 // (resident CTAs per SM) x (SM count), capped at the tile count.
 cudaError_t launch_elem(nfx_sim* s, int k) {
-    if (s->tet_variant == 1 && s->mesh.tile_tets == TILE_TETS) {
+    if (s->tet_variant == 1 && s->mesh.tile_tets <= TILE_TETS) {
         int& bps = s->pipe_bps[s->mat.model & 3];
-        if (bps < 0) bps = pipe_blocks_per_sm(s->mat.model);
+        if (bps < 0) bps = pipe_blocks_per_sm(s->mat.model, s->mesh.tile_tets);
         if (bps > 0) {
             const long long grid = std::min<long long>((long long)bps * s->sm_count, s->mesh.ntiles);
             return launch_tet_pass_pipe(s->mesh, s->st, s->mat, s->prm, k, (int)grid, s->stream);
@@ -218,7 +218,7 @@ int nfx_create(int device, nfx_sim** out) {
     if (const char* v = std::getenv("NFX_TET_KERNEL")) s->tet_variant = std::atoi(v) == 1 ? 1 : 0;
     if (const char* v = std::getenv("NFX_TILE_TETS")) {
         const int t = std::atoi(v);
-        if (t == 128 || t == 256 || t == 512) s->tile_tets = t;
+        if (t == 64 || t == 128 || t == 256 || t == 512) s->tile_tets = t;
     }
     // default integrator: the reference's xi = 0.005 (VelocityVerlet.cl:11)
     const double xi = 0.005;

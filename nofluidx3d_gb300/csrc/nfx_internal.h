@@ -19,7 +19,7 @@ constexpr int MAX_CONTACTS = 4;
 constexpr int TILE_TETS = 256;       // default tile size (the pipelined kernel's only size)
 constexpr int TILE_NODES_MAX = 256;  // 8-bit local corner indices
 // Tile sizes the one-CTA-per-tile kernel is built for; a tile has at most min(tile, 256) nodes.
-constexpr int TILE_SIZES[3] = {128, 256, 512};
+constexpr int TILE_SIZES[4] = {64, 128, 256, 512};
 constexpr int NODE_BLOCK = 256;
 
 // Fixed-point scale of the force accumulator: 2^40 (resolution 9.1e-13, range +-8.4e6).
@@ -140,8 +140,8 @@ cudaError_t launch_tet_pass(const MeshDev& m, const StateDev& s, const MaterialD
 // Persistent, bulk-copy-pipelined element pass: `grid` CTAs walk all tiles.
 cudaError_t launch_tet_pass_pipe(const MeshDev& m, const StateDev& s, const MaterialDev& mat, const StepParams& p,
                                  int t_offset, int grid, cudaStream_t stream);
-// Resident CTAs per SM of the pipelined element pass for a material model (0 on error).
-int pipe_blocks_per_sm(int model);
+// Resident CTAs per SM of the pipelined element pass for a material model and tile size.
+int pipe_blocks_per_sm(int model, int tile);
 enum NodeMode : int { NODE_UPDATE = 0, NODE_READOUT_ROW = 1, NODE_READOUT_VALUE = 2 };
 cudaError_t launch_node_pass(const MeshDev& m, const StateDev& s, const StepParams& p, int t_offset, int mode,
                              int readout_contact, cudaStream_t stream);

@@ -127,10 +127,11 @@ __device__ __forceinline__ bool fields_due(const StateDev& s, long long fields_e
 // Element pass, one CTA per tile (plain loads)
 // ------------------------------------------------------------------------------------------
 template <int MODEL, int TILE>
-__global__ void __launch_bounds__(TILE) k_tet_pass(MeshDev m, StateDev s, MaterialDev mat, long long fields_every,
+__global__ void __launch_bounds__(TILE, 65536 / (TILE * 64)) k_tet_pass(MeshDev m, StateDev s, MaterialDev mat, long long fields_every,
                                                    int t_offset) {
-    __shared__ float4 s_uh[TILE_NODES_MAX];
-    __shared__ float4 s_ul[TILE_NODES_MAX];
+    constexpr int NMAX = TILE < TILE_NODES_MAX ? TILE : TILE_NODES_MAX;
+    __shared__ float4 s_uh[NMAX];
+    __shared__ float4 s_ul[NMAX];
     __shared__ float4 s_cf[4 * TILE];  // corner forces, slot 4*local tet + corner
     __shared__ ushort4 s_inc[TILE];    // the tile's incidence list
 
@@ -183,32 +184,35 @@ __global__ void __launch_bounds__(TILE) k_tet_pass(MeshDev m, StateDev s, Materi
 // mbarrier; one tile ahead, all threads gather the tile's node displacements with cp.async.
 // While tile i is evaluated, tile i+1's node data and tile i+2's streams are in flight.
 // ------------------------------------------------------------------------------------------
+template <int TILE>
 struct StageLayout {
+    static constexpr int NMAX = TILE < TILE_NODES_MAX ? TILE : TILE_NODES_MAX;  // nodes per tile
     // byte offsets inside one stage (all multiples of 16)
-    static constexpr unsigned LCONN = 0;                       // uchar4[256]
-    static constexpr unsigned DMI_A = LCONN + 4 * TILE_TETS;   // float4[256]
-    static constexpr unsigned DMI_B = DMI_A + 16 * TILE_TETS;  // float4[256]
-    static constexpr unsigned DMI_C = DMI_B + 16 * TILE_TETS;  // float2[256]
-    static constexpr unsigned INC = DMI_C + 8 * TILE_TETS;     // ushort4[256]
-    static constexpr unsigned NODES = INC + 8 * TILE_TETS;     // uint2[258]
-    static constexpr unsigned UH = NODES + 8 * (TILE_NODES_MAX + 2);
-    static constexpr unsigned UL = UH + 16 * TILE_NODES_MAX;
-    static constexpr unsigned VP_A = UL + 16 * TILE_NODES_MAX;
-    static constexpr unsigned VP_B = VP_A + 16 * TILE_TETS;
-    static constexpr unsigned VP_C = VP_B + 16 * TILE_TETS;
+    static constexpr unsigned LCONN = 0;                  // uchar4[TILE]
+    static constexpr unsigned DMI_A = LCONN + 4 * TILE;   // float4[TILE]
+    static constexpr unsigned DMI_B = DMI_A + 16 * TILE;  // float4[TILE]
+    static constexpr unsigned DMI_C = DMI_B + 16 * TILE;  // float2[TILE]
+    static constexpr unsigned INC = DMI_C + 8 * TILE;     // ushort4[TILE]
+    static constexpr unsigned NODES = INC + 8 * TILE;     // uint2[NMAX + 2]
+    static constexpr unsigned UH = NODES + 8 * (NMAX + 2);
+    static constexpr unsigned UL = UH + 16 * NMAX;
+    static constexpr unsigned VP_A = UL + 16 * NMAX;
+    static constexpr unsigned VP_B = VP_A + 16 * TILE;
+    static constexpr unsigned VP_C = VP_B + 16 * TILE;
     static constexpr unsigned SIZE_ELASTIC = VP_A;
-    static constexpr unsigned SIZE_VP = VP_C + 8 * TILE_TETS;
+    static constexpr unsigned SIZE_VP = VP_C + 8 * TILE;
+    static_assert(UH % 16 == 0 && SIZE_VP % 16 == 0, "stage layout must be 16-byte aligned");
 };
-static_assert(StageLayout::UH % 16 == 0 && StageLayout::SIZE_VP % 16 == 0, "stage layout must be 16-byte aligned");
 
-constexpr unsigned PIPE_CF_BYTES = 16 * 4 * TILE_TETS;  // corner forces
-constexpr unsigned PIPE_HDR_BYTES = 64;                 // two mbarriers + two stage headers
+constexpr unsigned PIPE_HDR_BYTES = 64;  // two mbarriers + two stage headers
 
+template <int TILE>
 __host__ __device__ constexpr unsigned pipe_stage_bytes(int model) {
-    return model == MODEL_VP ? StageLayout::SIZE_VP : StageLayout::SIZE_ELASTIC;
+    return model == MODEL_VP ? StageLayout<TILE>::SIZE_VP : StageLayout<TILE>::SIZE_ELASTIC;
 }
+template <int TILE>
 __host__ __device__ constexpr unsigned pipe_smem_bytes(int model) {
-    return 2 * pipe_stage_bytes(model) + PIPE_CF_BYTES + PIPE_HDR_BYTES;
+    return 2 * pipe_stage_bytes<TILE>(model) + 16u * 4u * TILE + PIPE_HDR_BYTES;
 }
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -260,9 +264,10 @@ struct StageHdr {
 
 // Thread 0: issue the bulk copies of `tile` into stage `st` (header written first; the
 // mbarrier's release/acquire makes it visible to the waiting threads).
-template <int MODEL>
+template <int MODEL, int TILE>
 __device__ __forceinline__ void issue_tile(const MeshDev& m, const StateDev& s, int tile, unsigned char* st,
                                            StageHdr* hdr, unsigned long long* bar) {
+    using StageLayout = nfx::StageLayout<TILE>;
     const int tb = m.tile_tet_begin[tile], ntt = m.tile_tet_begin[tile + 1] - tb;
     const int nb = m.tile_node_begin[tile], nn = m.tile_node_begin[tile + 1] - nb;
     const int nb0 = nb & ~1;          // 16-byte aligned start of the node list
@@ -290,11 +295,13 @@ __device__ __forceinline__ void issue_tile(const MeshDev& m, const StateDev& s, 
 }
 
 // All threads: gather the node displacements of the tile in stage `st` (cp.async, one group).
+template <int TILE>
 __device__ __forceinline__ void gather_nodes(const StateDev& s, unsigned char* st, const StageHdr& h) {
+    using StageLayout = nfx::StageLayout<TILE>;
     const uint2* nodes = reinterpret_cast<const uint2*>(st + StageLayout::NODES) + h.noff;
     float4* uh = reinterpret_cast<float4*>(st + StageLayout::UH);
     float4* ul = reinterpret_cast<float4*>(st + StageLayout::UL);
-    for (int j = threadIdx.x; j < h.nn; j += TILE_TETS) {
+    for (int j = threadIdx.x; j < h.nn; j += TILE) {
         const unsigned g = nodes[j].x;
         cp_async16(uh + j, s.uh + g);
         cp_async16(ul + j, s.ul + g);
@@ -302,11 +309,13 @@ __device__ __forceinline__ void gather_nodes(const StateDev& s, unsigned char* s
     cp_async_commit();
 }
 
-template <int MODEL>
-__global__ void __launch_bounds__(TILE_TETS) k_tet_pass_pipe(MeshDev m, StateDev s, MaterialDev mat,
-                                                             long long fields_every, int t_offset) {
+template <int MODEL, int TILE>
+__global__ void __launch_bounds__(TILE) k_tet_pass_pipe(MeshDev m, StateDev s, MaterialDev mat,
+                                                        long long fields_every, int t_offset) {
+    using StageLayout = nfx::StageLayout<TILE>;
     extern __shared__ __align__(128) unsigned char smem[];
-    constexpr unsigned SB = pipe_stage_bytes(MODEL);
+    constexpr unsigned SB = pipe_stage_bytes<TILE>(MODEL);
+    constexpr unsigned PIPE_CF_BYTES = 16u * 4u * TILE;
     unsigned char* stage[2] = {smem, smem + SB};
     float4* s_cf = reinterpret_cast<float4*>(smem + 2 * SB);
     unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem + 2 * SB + PIPE_CF_BYTES);
@@ -323,13 +332,13 @@ __global__ void __launch_bounds__(TILE_TETS) k_tet_pass_pipe(MeshDev m, StateDev
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        issue_tile<MODEL>(m, s, first, stage[0], &hdr[0], &bar[0]);
-        if (first + G < m.ntiles) issue_tile<MODEL>(m, s, first + G, stage[1], &hdr[1], &bar[1]);
+        issue_tile<MODEL, TILE>(m, s, first, stage[0], &hdr[0], &bar[0]);
+        if (first + G < m.ntiles) issue_tile<MODEL, TILE>(m, s, first + G, stage[1], &hdr[1], &bar[1]);
         s_ok = mbar_wait_bounded(&bar[0], 0);
     }
     __syncthreads();
     bool ok = s_ok != 0;
-    if (ok) gather_nodes(s, stage[0], hdr[0]);
+    if (ok) gather_nodes<TILE>(s, stage[0], hdr[0]);
 
     for (int it = 0; ok; it++) {
         const int tile = first + it * G;
@@ -344,7 +353,7 @@ __global__ void __launch_bounds__(TILE_TETS) k_tet_pass_pipe(MeshDev m, StateDev
                 ok = false;
                 break;
             }
-            gather_nodes(s, stage[nxt], hdr[nxt]);
+            gather_nodes<TILE>(s, stage[nxt], hdr[nxt]);
             cp_async_wait<1>();
         } else {
             cp_async_wait<0>();
@@ -379,7 +388,7 @@ __global__ void __launch_bounds__(TILE_TETS) k_tet_pass_pipe(MeshDev m, StateDev
         __syncthreads();  // stage `cur` and the corner forces are free again
         if (j == 0 && tile + 2 * G < m.ntiles) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue_tile<MODEL>(m, s, tile + 2 * G, stage[cur], &hdr[cur], &bar[cur]);
+            issue_tile<MODEL, TILE>(m, s, tile + 2 * G, stage[cur], &hdr[cur], &bar[cur]);
         }
     }
     cp_async_wait<0>();
@@ -602,44 +611,65 @@ __global__ void k_vec_from_user(int np, float4* a, const long long* node_user, c
 // ------------------------------------------------------------------------------------------
 // Launchers
 // ------------------------------------------------------------------------------------------
-template <int MODEL>
+template <int MODEL, int TILE>
 static cudaError_t launch_pipe(const MeshDev& m, const StateDev& s, const MaterialDev& mat, const StepParams& p,
                                int t_offset, int grid, cudaStream_t st) {
-    const unsigned bytes = pipe_smem_bytes(MODEL);
+    const unsigned bytes = pipe_smem_bytes<TILE>(MODEL);
     static bool attr_set = false;  // per process; the attribute is per function
     if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_tet_pass_pipe<MODEL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(k_tet_pass_pipe<MODEL, TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)bytes);
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
-    k_tet_pass_pipe<MODEL><<<grid, TILE_TETS, bytes, st>>>(m, s, mat, p.fields_every, t_offset);
+    k_tet_pass_pipe<MODEL, TILE><<<grid, TILE, bytes, st>>>(m, s, mat, p.fields_every, t_offset);
     return cudaGetLastError();
 }
 
-int pipe_blocks_per_sm(int model) {
+template <int TILE>
+static int pipe_bps_tile(int model) {
     int n = 0;
     cudaError_t e = cudaSuccess;
     auto q = [&](auto kern, unsigned bytes) {
         e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, TILE_TETS, bytes);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, TILE, bytes);
     };
     switch (model) {
-        case MODEL_MR: q(k_tet_pass_pipe<MODEL_MR>, pipe_smem_bytes(MODEL_MR)); break;
-        case MODEL_SVK: q(k_tet_pass_pipe<MODEL_SVK>, pipe_smem_bytes(MODEL_SVK)); break;
-        case MODEL_SVKK: q(k_tet_pass_pipe<MODEL_SVKK>, pipe_smem_bytes(MODEL_SVKK)); break;
-        default: q(k_tet_pass_pipe<MODEL_VP>, pipe_smem_bytes(MODEL_VP)); break;
+        case MODEL_MR: q(k_tet_pass_pipe<MODEL_MR, TILE>, pipe_smem_bytes<TILE>(MODEL_MR)); break;
+        case MODEL_SVK: q(k_tet_pass_pipe<MODEL_SVK, TILE>, pipe_smem_bytes<TILE>(MODEL_SVK)); break;
+        case MODEL_SVKK: q(k_tet_pass_pipe<MODEL_SVKK, TILE>, pipe_smem_bytes<TILE>(MODEL_SVKK)); break;
+        default: q(k_tet_pass_pipe<MODEL_VP, TILE>, pipe_smem_bytes<TILE>(MODEL_VP)); break;
     }
     return e == cudaSuccess ? n : 0;
 }
 
+int pipe_blocks_per_sm(int model, int tile) {
+    switch (tile) {
+        case 64: return pipe_bps_tile<64>(model);
+        case 128: return pipe_bps_tile<128>(model);
+        case 256: return pipe_bps_tile<256>(model);
+        default: return 0;
+    }
+}
+
+template <int TILE>
+static cudaError_t launch_pipe_tile(const MeshDev& m, const StateDev& s, const MaterialDev& mat, const StepParams& p,
+                                    int t_offset, int grid, cudaStream_t st) {
+    switch (mat.model) {
+        case MODEL_MR: return launch_pipe<MODEL_MR, TILE>(m, s, mat, p, t_offset, grid, st);
+        case MODEL_SVK: return launch_pipe<MODEL_SVK, TILE>(m, s, mat, p, t_offset, grid, st);
+        case MODEL_SVKK: return launch_pipe<MODEL_SVKK, TILE>(m, s, mat, p, t_offset, grid, st);
+        case MODEL_VP: return launch_pipe<MODEL_VP, TILE>(m, s, mat, p, t_offset, grid, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
 cudaError_t launch_tet_pass_pipe(const MeshDev& m, const StateDev& s, const MaterialDev& mat, const StepParams& p,
                                  int t_offset, int grid, cudaStream_t st) {
-    switch (mat.model) {
-        case MODEL_MR: return launch_pipe<MODEL_MR>(m, s, mat, p, t_offset, grid, st);
-        case MODEL_SVK: return launch_pipe<MODEL_SVK>(m, s, mat, p, t_offset, grid, st);
-        case MODEL_SVKK: return launch_pipe<MODEL_SVKK>(m, s, mat, p, t_offset, grid, st);
-        case MODEL_VP: return launch_pipe<MODEL_VP>(m, s, mat, p, t_offset, grid, st);
+    switch (m.tile_tets) {
+        case 64: return launch_pipe_tile<64>(m, s, mat, p, t_offset, grid, st);
+        case 128: return launch_pipe_tile<128>(m, s, mat, p, t_offset, grid, st);
+        case 256: return launch_pipe_tile<256>(m, s, mat, p, t_offset, grid, st);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -661,6 +691,7 @@ static cudaError_t launch_tile(const MeshDev& m, const StateDev& s, const Materi
 cudaError_t launch_tet_pass(const MeshDev& m, const StateDev& s, const MaterialDev& mat, const StepParams& p,
                             int t_offset, cudaStream_t st) {
     switch (m.tile_tets) {
+        case 64: return launch_tile<64>(m, s, mat, p, t_offset, st);
         case 128: return launch_tile<128>(m, s, mat, p, t_offset, st);
         case 256: return launch_tile<256>(m, s, mat, p, t_offset, st);
         case 512: return launch_tile<512>(m, s, mat, p, t_offset, st);

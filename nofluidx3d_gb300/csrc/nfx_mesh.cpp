@@ -53,8 +53,8 @@ struct Quant {
 
 bool build_mesh_plan(int64_t np, int64_t nt, const double* P, const uint32_t* T, int tile_tets, MeshPlan& plan,
                      std::string& err) {
-    if (tile_tets != 128 && tile_tets != 256 && tile_tets != 512) {
-        err = "tile size must be 128, 256 or 512";
+    if (tile_tets != 64 && tile_tets != 128 && tile_tets != 256 && tile_tets != 512) {
+        err = "tile size must be 64, 128, 256 or 512";
         return false;
     }
     if (np <= 0 || nt <= 0) {
