@@ -174,6 +174,51 @@ int nfx_profile_steps(nfx_sim* sim, int64_t nsteps, float* tet_ms, float* node_m
 /* Number of mesh tiles and distinct-node entries (diagnostics for the tile layout). */
 int nfx_mesh_info(nfx_sim* sim, int64_t* ntiles, int64_t* tile_nodes);
 
+/* ------------------------------------------------------------------------------------------
+ * Batched cells. The reference advances one cell per Simulation (nofluidx3d/Simulation.py:35);
+ * a batch advances many independent cells of uneven size and material together: one element-pass
+ * launch and one node-pass launch per step for all cells, captured as a CUDA graph. All cells of
+ * a batch use one material model; each has its own parameters, contacts, integrator settings and
+ * force curve. Set-up calls come before nfx_batch_finalize; stepping and readback after.
+ * ------------------------------------------------------------------------------------------ */
+typedef struct nfx_batch nfx_batch;
+
+/* tile_tets: 64, 128, 256 or 512 tetrahedra per tile, or 0 to let nfx_batch_finalize time a
+ * representative sub-batch with 64, 128 and 256 and keep the fastest. */
+int nfx_batch_create(int device, int tile_tets, nfx_batch** out);
+int nfx_batch_destroy(nfx_batch* batch);
+/* Adds a cell (layouts as nfx_set_mesh); *cell receives its index. */
+int nfx_batch_add_cell(nfx_batch* batch, int64_t np, int64_t nt, const double* points, const uint32_t* tets, int* cell);
+/* Per-cell material, as nfx_set_tetra / nfx_set_viscoplastic. */
+int nfx_batch_set_tetra(nfx_batch* batch, int cell, int model, double youngs_modulus, double poisson_ratio,
+                        double mooney_rivlin_ratio);
+int nfx_batch_set_viscoplastic(nfx_batch* batch, int cell, const double* par8);
+/* Per-cell contact (schedule only), as nfx_add_contact. */
+int nfx_batch_add_contact(nfx_batch* batch, int cell, int kind, double k, double radius, double p0, double v,
+                          double tmove, int* id);
+/* Per-cell integrator, as nfx_set_integrator. */
+int nfx_batch_set_integrator(nfx_batch* batch, int cell, double xi, int fix_top_bottom);
+/* Records contact index `contact` of every cell every `every` steps into max_rows rows per cell. */
+int nfx_batch_set_record(nfx_batch* batch, int contact, int64_t every, int64_t max_rows);
+/* Builds the cells' plans on host threads (after autotuning the tile size when requested),
+ * uploads them and zeroes the state. */
+int nfx_batch_finalize(nfx_batch* batch);
+/* Enqueues nsteps steps of every cell. */
+int nfx_batch_step(nfx_batch* batch, int64_t nsteps);
+/* nfx_batch_step bracketed by CUDA events on the batch's stream; waits; *ms = device time. */
+int nfx_batch_time_steps(nfx_batch* batch, int64_t nsteps, float* ms);
+/* Records the row of the current time for every cell (see nfx_record_now). */
+int nfx_batch_record_now(nfx_batch* batch);
+/* Force curve of one cell (rows of t, indentation, force); *n_rows = rows available. */
+int nfx_batch_get_curve(nfx_batch* batch, int cell, double* rows, int64_t max_rows, int64_t* n_rows);
+/* Node positions of one cell, double[3*np] SoA in the cell's user order. */
+int nfx_batch_get_points(nfx_batch* batch, int cell, double* out);
+int nfx_batch_status(nfx_batch* batch, uint32_t* flags, int clear);
+/* Cells, total tetrahedra and nodes, tile size in use. */
+int nfx_batch_info(nfx_batch* batch, int64_t* cells, int64_t* tets, int64_t* nodes, int* tile_tets);
+/* The autotuner's candidates and their times (ms for 10 steps of the sub-batch). */
+int nfx_batch_tuning(nfx_batch* batch, int* tiles, float* ms, int max_n, int* n);
+
 /* Indenter force of one contact on node positions the caller keeps in device memory, written
  * to one double in device memory. This entry point has no counterpart in the reference.
  *

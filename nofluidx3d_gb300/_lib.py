@@ -68,6 +68,24 @@ _SIGS = {
     "nfx_mesh_info": ([_vp, C.POINTER(_i64), C.POINTER(_i64)], C.c_int),
     "nfx_indenter_force_noalloc": ([C.c_int, _i64, _vp, C.c_int, C.c_double, C.c_double, C.c_double, _vp, _vp],
                                    C.c_int),
+    "nfx_batch_create": ([C.c_int, C.c_int, C.POINTER(_vp)], C.c_int),
+    "nfx_batch_destroy": ([_vp], C.c_int),
+    "nfx_batch_add_cell": ([_vp, _i64, _i64, _vp, _vp, C.POINTER(C.c_int)], C.c_int),
+    "nfx_batch_set_tetra": ([_vp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double], C.c_int),
+    "nfx_batch_set_viscoplastic": ([_vp, C.c_int, _vp], C.c_int),
+    "nfx_batch_add_contact": ([_vp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                               C.POINTER(C.c_int)], C.c_int),
+    "nfx_batch_set_integrator": ([_vp, C.c_int, C.c_double, C.c_int], C.c_int),
+    "nfx_batch_set_record": ([_vp, C.c_int, _i64, _i64], C.c_int),
+    "nfx_batch_finalize": ([_vp], C.c_int),
+    "nfx_batch_step": ([_vp, _i64], C.c_int),
+    "nfx_batch_time_steps": ([_vp, _i64, C.POINTER(C.c_float)], C.c_int),
+    "nfx_batch_record_now": ([_vp], C.c_int),
+    "nfx_batch_get_curve": ([_vp, C.c_int, _vp, _i64, C.POINTER(_i64)], C.c_int),
+    "nfx_batch_get_points": ([_vp, C.c_int, _vp], C.c_int),
+    "nfx_batch_status": ([_vp, C.POINTER(C.c_uint32), C.c_int], C.c_int),
+    "nfx_batch_info": ([_vp, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64), C.POINTER(C.c_int)], C.c_int),
+    "nfx_batch_tuning": ([_vp, _vp, _vp, C.c_int, C.POINTER(C.c_int)], C.c_int),
 }
 
 

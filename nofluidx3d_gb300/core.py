@@ -16,7 +16,7 @@ from . import _lib
 from ._lib import (CONTACT_PLANE, CONTACT_SPHERE, CONTACT_SUBSTRATE, FIELD_PLASTIC_STRAIN, FIELD_PRESSURE,
                    FIELD_VON_MISES, MODEL_MR, MODEL_SVK, MODEL_SVKK, MODEL_VP, NfxError, check)
 
-__all__ = ["CellSim", "NfxError", "MODEL_MR", "MODEL_SVK", "MODEL_SVKK", "MODEL_VP", "CONTACT_SUBSTRATE",
+__all__ = ["CellSim", "Batch", "NfxError", "MODEL_MR", "MODEL_SVK", "MODEL_SVKK", "MODEL_VP", "CONTACT_SUBSTRATE",
            "CONTACT_PLANE", "CONTACT_SPHERE", "FIELD_VON_MISES", "FIELD_PRESSURE", "FIELD_PLASTIC_STRAIN",
            "to_soa", "from_soa"]
 
@@ -204,3 +204,95 @@ class CellSim:
         a, b = C.c_int64(), C.c_int64()
         check(self._L.nfx_mesh_info(self._h, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+
+class Batch:
+    """Many independent cells advanced together (nfx_batch_*, include/nfx.h)."""
+
+    def __init__(self, device: int = 0, tile_tets: int = 0):
+        self._L = _lib.load()
+        h = C.c_void_p()
+        check(self._L.nfx_batch_create(int(device), int(tile_tets), C.byref(h)))
+        self._h = h
+        self.cells: list[tuple[int, int]] = []  # (np, nt) per cell
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._L.nfx_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_cell(self, points: np.ndarray, tets: np.ndarray) -> int:
+        pts = to_soa(points, np.float64)
+        tt = to_soa(tets, np.uint32)
+        cid = C.c_int(-1)
+        np_, nt = int(np.asarray(points).shape[0]), int(np.asarray(tets).shape[0])
+        check(self._L.nfx_batch_add_cell(self._h, np_, nt, _ptr(pts), _ptr(tt), C.byref(cid)))
+        self.cells.append((np_, nt))
+        return cid.value
+
+    def set_tetra(self, cell: int, model: int, youngs: float, poisson: float, mr_ratio: float = 1.0) -> None:
+        check(self._L.nfx_batch_set_tetra(self._h, int(cell), int(model), float(youngs), float(poisson), float(mr_ratio)))
+
+    def set_viscoplastic(self, cell: int, par: Sequence[float]) -> None:
+        p = np.ascontiguousarray(par, np.float64)
+        check(self._L.nfx_batch_set_viscoplastic(self._h, int(cell), _ptr(p)))
+
+    def add_contact(self, cell: int, kind: int, k: float, radius: float = 0.0, p0: float = 0.0, v: float = 0.0,
+                    tmove: float = float("inf")) -> int:
+        cid = C.c_int(-1)
+        check(self._L.nfx_batch_add_contact(self._h, int(cell), int(kind), float(k), float(radius), float(p0),
+                                            float(v), float(tmove), C.byref(cid)))
+        return cid.value
+
+    def set_integrator(self, cell: int, xi: float, fix_top_bottom: bool = False) -> None:
+        check(self._L.nfx_batch_set_integrator(self._h, int(cell), float(xi), int(bool(fix_top_bottom))))
+
+    def set_record(self, contact: int, every: int, max_rows: int) -> None:
+        check(self._L.nfx_batch_set_record(self._h, int(contact), int(every), int(max_rows)))
+
+    def finalize(self) -> None:
+        check(self._L.nfx_batch_finalize(self._h))
+
+    def step(self, n: int) -> None:
+        check(self._L.nfx_batch_step(self._h, int(n)))
+
+    def time_steps(self, n: int) -> float:
+        ms = C.c_float()
+        check(self._L.nfx_batch_time_steps(self._h, int(n), C.byref(ms)))
+        return ms.value
+
+    def record_now(self) -> None:
+        check(self._L.nfx_batch_record_now(self._h))
+
+    def curve(self, cell: int) -> np.ndarray:
+        n = C.c_int64()
+        check(self._L.nfx_batch_get_curve(self._h, int(cell), None, 0, C.byref(n)))
+        out = np.zeros((max(n.value, 1), 3), np.float64)
+        check(self._L.nfx_batch_get_curve(self._h, int(cell), _ptr(out), n.value, C.byref(n)))
+        return out[:n.value]
+
+    def points(self, cell: int) -> np.ndarray:
+        out = np.empty(3 * self.cells[cell][0], np.float64)
+        check(self._L.nfx_batch_get_points(self._h, int(cell), _ptr(out)))
+        return from_soa(out, 3)
+
+    def status(self, clear: bool = False) -> int:
+        f = C.c_uint32()
+        check(self._L.nfx_batch_status(self._h, C.byref(f), int(bool(clear))))
+        return f.value
+
+    def info(self) -> dict:
+        a, b, c, d = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int()
+        check(self._L.nfx_batch_info(self._h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))
+        tiles = (C.c_int * 8)()
+        ms = (C.c_float * 8)()
+        n = C.c_int()
+        check(self._L.nfx_batch_tuning(self._h, C.cast(tiles, C.c_void_p), C.cast(ms, C.c_void_p), 8, C.byref(n)))
+        return {"cells": a.value, "tets": b.value, "nodes": c.value, "tile_tets": d.value,
+                "tuning": [(tiles[i], ms[i]) for i in range(n.value)]}

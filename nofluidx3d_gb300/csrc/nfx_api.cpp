@@ -71,7 +71,7 @@ struct nfx_sim {
     bool graph_valid = false;
     int sm_count = 1;
     int tet_variant = 0;                   // 1: persistent pipelined element pass, 0: one CTA per tile
-    int tile_tets = TILE_TETS;             // tetrahedra per tile (64, 128, 256 or 512)
+    int tile_tets = DEFAULT_TILE_TETS;     // tetrahedra per tile (64, 128, 256 or 512)
     int pipe_bps[4] = {-1, -1, -1, -1};    // resident CTAs per SM of the pipelined kernel, per model
 };
 

@@ -16,7 +16,8 @@ constexpr int MAX_CONTACTS = 4;
 // A tile is a run of consecutive tetrahedra (after reordering) processed by one CTA. Its
 // distinct nodes are listed once, so the per-tetra connectivity is four 8-bit local indices
 // and the tile's nodal forces are summed in shared memory before one flush per node.
-constexpr int TILE_TETS = 256;       // default tile size (the pipelined kernel's only size)
+constexpr int TILE_TETS = 256;          // largest tile of the pipelined kernel
+constexpr int DEFAULT_TILE_TETS = 128;  // fastest measured on GB300 (R=64 viscoplastic cell)
 constexpr int TILE_NODES_MAX = 256;  // 8-bit local corner indices
 // Tile sizes the one-CTA-per-tile kernel is built for; a tile has at most min(tile, 256) nodes.
 constexpr int TILE_SIZES[4] = {64, 128, 256, 512};
@@ -131,8 +132,40 @@ struct StepParams {
     int fix_a, fix_b;          // internal ids of the pinned nodes, -1 if none
 };
 
+// ---------------------------------------------------------------------------------------
+// Batched cells: one set of concatenated tile/tetra/node arrays for many independent cells,
+// with per-cell parameters looked up per tile (element pass) and per node block (node pass).
+// Each cell's nodes occupy whole node blocks, so a node block belongs to exactly one cell.
+// ---------------------------------------------------------------------------------------
+struct CellDev {
+    MaterialDev mat;
+    int n_contacts;
+    ContactDev c[MAX_CONTACTS];
+    float vv_a, vv_hb, vv_dm;
+    int fix_a, fix_b;             // global node ids of the pinned nodes, -1 if none
+    int record_contact;           // -1: none
+    int node_begin, node_end;     // the cell's nodes in the global arrays
+    int block_begin, block_end;   // the cell's node blocks
+};
+
+struct BatchDev {
+    const CellDev* cells;
+    const int* tile_cell;        // per tile
+    const int* block_cell;       // per node block
+    unsigned* cell_counter;      // per cell: blocks finished in the readout reduction
+    double* curves;              // per cell: max_rows rows of (t, indentation, force)
+    long long record_every, max_rows, fields_every;
+};
+
 // Sets the message nfx_last_error() returns on this thread (nfx_api.cpp).
 void set_error(const std::string& msg);
+
+// Batched launches (nfx_kernels.cu): element pass over all tiles of all cells, node pass over
+// all node blocks.
+cudaError_t launch_tet_pass_batch(const MeshDev& m, const StateDev& s, const BatchDev& b, int model, int t_offset,
+                                  cudaStream_t stream);
+cudaError_t launch_node_pass_batch(const MeshDev& m, const StateDev& s, const BatchDev& b, int nblocks, int t_offset,
+                                   int mode, cudaStream_t stream);
 
 // Kernel launchers (nfx_kernels.cu). All enqueue on `stream` and return cudaGetLastError().
 cudaError_t launch_tet_pass(const MeshDev& m, const StateDev& s, const MaterialDev& mat, const StepParams& p,

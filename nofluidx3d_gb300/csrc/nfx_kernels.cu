@@ -126,9 +126,11 @@ __device__ __forceinline__ bool fields_due(const StateDev& s, long long fields_e
 // ------------------------------------------------------------------------------------------
 // Element pass, one CTA per tile (plain loads)
 // ------------------------------------------------------------------------------------------
-template <int MODEL, int TILE>
-__global__ void __launch_bounds__(TILE, 65536 / (TILE * 64)) k_tet_pass(MeshDev m, StateDev s, MaterialDev mat, long long fields_every,
-                                                   int t_offset) {
+// BATCHED: tiles of many cells in one launch; each tile takes its cell's material from the
+// batch's parameter table instead of `mat`.
+template <int MODEL, int TILE, bool BATCHED>
+__global__ void __launch_bounds__(TILE, 65536 / (TILE * 64))
+    k_tet_pass(MeshDev m, StateDev s, MaterialDev mat, BatchDev bd, long long fields_every, int t_offset) {
     constexpr int NMAX = TILE < TILE_NODES_MAX ? TILE : TILE_NODES_MAX;
     __shared__ float4 s_uh[NMAX];
     __shared__ float4 s_ul[NMAX];
@@ -169,6 +171,7 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * 64)) k_tet_pass(MeshDev 
         s_uh[j] = s.uh[node.x];
         s_ul[j] = s.ul[node.x];
     }
+    if (BATCHED) mat = bd.cells[bd.tile_cell[b]].mat;
     __syncthreads();
     if (act) element_eval<MODEL>(j, t, lc, da, db, dc, pa, pb, pc, s_uh, s_ul, s_cf, s, mat, wf);
     __syncthreads();
@@ -496,6 +499,52 @@ __device__ __forceinline__ double contact_force(const ContactDev& c, double w, c
     return fy;
 }
 
+// One node: element force from the fixed-point accumulator, the contacts in order (returns the
+// readout value -f_y of contact rc), and in update mode the damped velocity-Verlet step with the
+// displacement carried as hi + lo, the FIXED_TOP_BOTTOM pin, and the accumulator reset.
+__device__ __forceinline__ double node_step(const MeshDev& m, const StateDev& s, int i, long long t,
+                                           const ContactDev* cs, int nc, int rc, float vv_a, float vv_hb,
+                                           float vv_dm, int fix_a, int fix_b, bool update) {
+    const long long np = m.np;
+    float4 f = make_float4(__ll2float_rn((long long)s.facc[i]) * FORCE_FIX_INV,
+                           __ll2float_rn((long long)s.facc[np + i]) * FORCE_FIX_INV,
+                           __ll2float_rn((long long)s.facc[2 * np + i]) * FORCE_FIX_INV, 0.f);
+    const float4 xh = m.Xh[i];
+    float4 uh = s.uh[i], ul = s.ul[i];
+    double ro = 0.0;
+    for (int c = 0; c < nc; c++) {
+        const double w = contact_pos(cs[c], t);
+        const double fy = contact_force(cs[c], w, xh, m.Xl + i, uh, ul, f);
+        if (c == rc) ro = -fy;
+    }
+    if (update) {
+        float4 v = s.v[i];
+        const float4 fo = s.fo[i];
+        v.x = vv_a * v.x + vv_hb * (f.x + fo.x);
+        v.y = vv_a * v.y + vv_hb * (f.y + fo.y);
+        v.z = vv_a * v.z + vv_hb * (f.z + fo.z);
+        df_add(uh.x, ul.x, vv_dm * v.x + 0.5f * f.x);
+        df_add(uh.y, ul.y, vv_dm * v.y + 0.5f * f.y);
+        df_add(uh.z, ul.z, vv_dm * v.z + 0.5f * f.z);
+        if (i == fix_a || i == fix_b) {  // VelocityVerlet.cl:17-22: x = z = 0
+            const float4 xl = m.Xl[i];
+            uh.x = -xh.x;
+            ul.x = -xl.x;
+            uh.z = -xh.z;
+            ul.z = -xl.z;
+        }
+        if (!isfinite(uh.x + uh.y + uh.z + v.x + v.y + v.z)) atomicOr(s.status, STATUS_NONFINITE);
+        s.uh[i] = uh;
+        s.ul[i] = ul;
+        s.v[i] = v;
+        s.fo[i] = make_float4(f.x, f.y, f.z, 0.f);
+        s.facc[i] = 0ull;
+        s.facc[np + i] = 0ull;
+        s.facc[2 * np + i] = 0ull;
+    }
+    return ro;
+}
+
 __global__ void __launch_bounds__(NODE_BLOCK) k_node_pass(MeshDev m, StateDev s, StepParams p, int t_offset,
                                                           int mode, int readout_contact) {
     const int i = blockIdx.x * NODE_BLOCK + threadIdx.x;
@@ -518,48 +567,72 @@ __global__ void __launch_bounds__(NODE_BLOCK) k_node_pass(MeshDev m, StateDev s,
         }
     }
     double ro = 0.0;
-    if (i < m.np) {
-        const long long np = m.np;
-        float4 f = make_float4(__ll2float_rn((long long)s.facc[i]) * FORCE_FIX_INV,
-                               __ll2float_rn((long long)s.facc[np + i]) * FORCE_FIX_INV,
-                               __ll2float_rn((long long)s.facc[2 * np + i]) * FORCE_FIX_INV, 0.f);
-        const float4 xh = m.Xh[i];
-        float4 uh = s.uh[i], ul = s.ul[i];
-        for (int c = 0; c < p.n_contacts; c++) {
-            const double w = contact_pos(p.c[c], t);
-            const double fy = contact_force(p.c[c], w, xh, m.Xl + i, uh, ul, f);
-            if (c == rc) ro = -fy;
-        }
-        if (mode == NODE_UPDATE) {
-            float4 v = s.v[i];
-            const float4 fo = s.fo[i];
-            v.x = p.vv_a * v.x + p.vv_hb * (f.x + fo.x);
-            v.y = p.vv_a * v.y + p.vv_hb * (f.y + fo.y);
-            v.z = p.vv_a * v.z + p.vv_hb * (f.z + fo.z);
-            df_add(uh.x, ul.x, p.vv_dm * v.x + 0.5f * f.x);
-            df_add(uh.y, ul.y, p.vv_dm * v.y + 0.5f * f.y);
-            df_add(uh.z, ul.z, p.vv_dm * v.z + 0.5f * f.z);
-            if (i == p.fix_a || i == p.fix_b) {  // VelocityVerlet.cl:17-22: x = z = 0
-                const float4 xl = m.Xl[i];
-                uh.x = -xh.x;
-                ul.x = -xl.x;
-                uh.z = -xh.z;
-                ul.z = -xl.z;
-            }
-            if (!isfinite(uh.x + uh.y + uh.z + v.x + v.y + v.z)) atomicOr(s.status, STATUS_NONFINITE);
-            s.uh[i] = uh;
-            s.ul[i] = ul;
-            s.v[i] = v;
-            s.fo[i] = make_float4(f.x, f.y, f.z, 0.f);
-            s.facc[i] = 0ull;
-            s.facc[np + i] = 0ull;
-            s.facc[2 * np + i] = 0ull;
-        }
-    }
+    if (i < m.np)
+        ro = node_step(m, s, i, t, p.c, p.n_contacts, rc, p.vv_a, p.vv_hb, p.vv_dm, p.fix_a, p.fix_b,
+                       mode == NODE_UPDATE);
     if (rec) {
         double ind = 0.0;
         if (rc >= 0 && rc < p.n_contacts) ind = contact_pos(p.c[rc], 0) - contact_pos(p.c[rc], t);
         grid_sum_finish(s, ro, mode == NODE_READOUT_VALUE, row, t, ind);
+    }
+}
+
+// Batched node pass: block -> cell, the cell's parameters from the batch table, and a per-cell
+// fixed-order readout (the cell's last block to finish sums the cell's block partials in order).
+__global__ void __launch_bounds__(NODE_BLOCK) k_node_pass_batch(MeshDev m, StateDev s, BatchDev bd, int t_offset,
+                                                                int mode) {
+    __shared__ double s_w[NODE_BLOCK / 32];
+    __shared__ int s_last;
+    const int cell = bd.block_cell[blockIdx.x];
+    const CellDev& C = bd.cells[cell];
+    const int i = blockIdx.x * NODE_BLOCK + threadIdx.x;
+    const long long t = *s.time + t_offset;
+    const int rc = C.record_contact;
+    bool rec = rc >= 0 && bd.record_every > 0 && (t % bd.record_every) == 0;
+    long long row = 0;
+    if (rec) {
+        row = t / bd.record_every;
+        if (row >= bd.max_rows) {
+            if (threadIdx.x == 0) atomicOr(s.status, STATUS_CURVE_FULL);
+            rec = false;
+        }
+    }
+    double ro = 0.0;
+    if (i < C.node_end)
+        ro = node_step(m, s, i, t, C.c, C.n_contacts, rc, C.vv_a, C.vv_hb, C.vv_dm, C.fix_a, C.fix_b,
+                       mode == NODE_UPDATE);
+    if (!rec) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    ro = warp_sum_d(ro);
+    if (lane == 0) s_w[warp] = ro;
+    __syncthreads();
+    if (warp == 0) {
+        double x = lane < NODE_BLOCK / 32 ? s_w[lane] : 0.0;
+        x = warp_sum_d(x);
+        if (lane == 0) {
+            s.partials[blockIdx.x] = x;
+            __threadfence();
+            const unsigned prev = atomicAdd(bd.cell_counter + cell, 1u);
+            s_last = prev == (unsigned)(C.block_end - C.block_begin - 1);
+        }
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    const volatile double* part = s.partials;
+    double acc = 0.0;
+    for (int k = C.block_begin + threadIdx.x; k < C.block_end; k += NODE_BLOCK) acc += part[k];
+    acc = warp_sum_d(acc);
+    if (lane == 0) s_w[warp] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tot = 0.0;
+        for (int w = 0; w < NODE_BLOCK / 32; w++) tot += s_w[w];
+        double* r = bd.curves + 3 * ((long long)cell * bd.max_rows + row);
+        r[0] = (double)t;
+        r[1] = contact_pos(C.c[rc], 0) - contact_pos(C.c[rc], t);
+        r[2] = tot;
+        bd.cell_counter[cell] = 0u;
     }
 }
 
@@ -679,10 +752,10 @@ static cudaError_t launch_tile(const MeshDev& m, const StateDev& s, const Materi
                                int t_offset, cudaStream_t st) {
     const dim3 grid((unsigned)m.ntiles), block(TILE);
     switch (mat.model) {
-        case MODEL_MR: k_tet_pass<MODEL_MR, TILE><<<grid, block, 0, st>>>(m, s, mat, p.fields_every, t_offset); break;
-        case MODEL_SVK: k_tet_pass<MODEL_SVK, TILE><<<grid, block, 0, st>>>(m, s, mat, p.fields_every, t_offset); break;
-        case MODEL_SVKK: k_tet_pass<MODEL_SVKK, TILE><<<grid, block, 0, st>>>(m, s, mat, p.fields_every, t_offset); break;
-        case MODEL_VP: k_tet_pass<MODEL_VP, TILE><<<grid, block, 0, st>>>(m, s, mat, p.fields_every, t_offset); break;
+        case MODEL_MR: k_tet_pass<MODEL_MR, TILE, false><<<grid, block, 0, st>>>(m, s, mat, BatchDev{}, p.fields_every, t_offset); break;
+        case MODEL_SVK: k_tet_pass<MODEL_SVK, TILE, false><<<grid, block, 0, st>>>(m, s, mat, BatchDev{}, p.fields_every, t_offset); break;
+        case MODEL_SVKK: k_tet_pass<MODEL_SVKK, TILE, false><<<grid, block, 0, st>>>(m, s, mat, BatchDev{}, p.fields_every, t_offset); break;
+        case MODEL_VP: k_tet_pass<MODEL_VP, TILE, false><<<grid, block, 0, st>>>(m, s, mat, BatchDev{}, p.fields_every, t_offset); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -697,6 +770,38 @@ cudaError_t launch_tet_pass(const MeshDev& m, const StateDev& s, const MaterialD
         case 512: return launch_tile<512>(m, s, mat, p, t_offset, st);
         default: return cudaErrorInvalidValue;
     }
+}
+
+template <int TILE>
+static cudaError_t launch_tile_batch(const MeshDev& m, const StateDev& s, const BatchDev& b, int model, int t_offset,
+                                     cudaStream_t st) {
+    const dim3 grid((unsigned)m.ntiles), block(TILE);
+    const MaterialDev mat{};
+    switch (model) {
+        case MODEL_MR: k_tet_pass<MODEL_MR, TILE, true><<<grid, block, 0, st>>>(m, s, mat, b, b.fields_every, t_offset); break;
+        case MODEL_SVK: k_tet_pass<MODEL_SVK, TILE, true><<<grid, block, 0, st>>>(m, s, mat, b, b.fields_every, t_offset); break;
+        case MODEL_SVKK: k_tet_pass<MODEL_SVKK, TILE, true><<<grid, block, 0, st>>>(m, s, mat, b, b.fields_every, t_offset); break;
+        case MODEL_VP: k_tet_pass<MODEL_VP, TILE, true><<<grid, block, 0, st>>>(m, s, mat, b, b.fields_every, t_offset); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tet_pass_batch(const MeshDev& m, const StateDev& s, const BatchDev& b, int model, int t_offset,
+                                  cudaStream_t st) {
+    switch (m.tile_tets) {
+        case 64: return launch_tile_batch<64>(m, s, b, model, t_offset, st);
+        case 128: return launch_tile_batch<128>(m, s, b, model, t_offset, st);
+        case 256: return launch_tile_batch<256>(m, s, b, model, t_offset, st);
+        case 512: return launch_tile_batch<512>(m, s, b, model, t_offset, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_node_pass_batch(const MeshDev& m, const StateDev& s, const BatchDev& b, int nblocks, int t_offset,
+                                   int mode, cudaStream_t st) {
+    k_node_pass_batch<<<nblocks, NODE_BLOCK, 0, st>>>(m, s, b, t_offset, mode);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_node_pass(const MeshDev& m, const StateDev& s, const StepParams& p, int t_offset, int mode,

@@ -105,6 +105,20 @@ class Workload:
         sim.set_record(self.record_contact, self.record_every, rows)
         return m
 
+    def add_to_batch(self, batch, mesh: CellMesh | None = None) -> int:
+        """Add this cell (mesh, material, contacts, integrator) to a core.Batch; returns its index."""
+        m = mesh if mesh is not None else self.mesh()
+        cell = batch.add_cell(m.points, m.tets)
+        if self.material == "mr_vp":
+            batch.set_viscoplastic(cell, self.vp_params())
+        else:
+            model, E, nu, mr = self.tetra_params()
+            batch.set_tetra(cell, model, E, nu, mr)
+        for c in self.contacts():
+            batch.add_contact(cell, c["kind"], c["k"], c["radius"], c["p0"], c["v"], c["tmove"])
+        batch.set_integrator(cell, self.xi, False)
+        return cell
+
     def with_(self, **kw) -> "Workload":
         return replace(self, **kw)
 
@@ -136,3 +150,29 @@ def plain_large_r48() -> Workload:
 
 WORKLOADS = {"plain-small": plain_small, "plain-large": plain_large, "plain-large-1m": plain_large_1m,
              "plain-large-r48": plain_large_r48}
+
+
+def batched_cells(n: int = 256, seed: int = 0, r_range=(6.0, 40.0), steps: int = 20000) -> list[Workload]:
+    """The batched population: n cells with radius log-uniform in r_range, per-cell jitter seed
+    (seed + cell index), and per-cell material drawn log-uniform — shear modulus 2e-4..5e-3,
+    bulk/shear ratio 5..50, yield stress 5e-5..1e-3, plastic viscosity 1e-2..1e-1 — with the
+    viscoplastic law (elastic part Neo-Hookean: mu1 = shear modulus, mu2 = 0). Each cell rests
+    on a substrate and is indented by a sphere of a quarter of its radius at 1e-4 per step."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+
+    def logu(lo, hi, size):
+        return np.exp(rng.uniform(np.log(lo), np.log(hi), size))
+
+    R = logu(*r_range, n)
+    mu = logu(2e-4, 5e-3, n)
+    ratio = logu(5.0, 50.0, n)
+    Y = logu(5e-5, 1e-3, n)
+    eta = logu(1e-2, 1e-1, n)
+    out = []
+    for i in range(n):
+        out.append(Workload(f"batched cell {i}", radius=float(R[i]), material="mr_vp", C10=float(mu[i]) / 2.0,
+                            C01=0.0, K=float(mu[i] * ratio[i]), yield_stress=float(Y[i]), viscosity=float(eta[i]),
+                            indenter="sphere", sphere_radius=float(R[i]) / 4.0, steps=steps, seed=seed + i))
+    return out

@@ -1,0 +1,76 @@
+"""Batched cells (nfx_batch_*): every cell of a batch evolves exactly as the same cell run alone
+through the plain path, and the autotuned batch agrees with the FP64 oracle."""
+
+import numpy as np
+import pytest
+
+import oracle as O
+from nofluidx3d_gb300.core import Batch, CellSim
+from nofluidx3d_gb300.workloads import Workload, batched_cells
+from tests.helpers import oracle_problem, rel_curve, rel_traj
+
+pytestmark = pytest.mark.gpu
+
+
+def small_population():
+    cells = batched_cells(4, seed=7, r_range=(2.5, 4.0), steps=250)
+    # faster indentation so short runs produce forces; one elastic-only look-alike is not mixed in
+    return [w.with_(speed=1e-3, record_every=50) for w in cells]
+
+
+def test_batch_equals_cells_run_alone_bitwise(monkeypatch):
+    """Same tile size as the plain path's default (128): same plans, same arithmetic."""
+    monkeypatch.delenv("NFX_TILE_TETS", raising=False)
+    monkeypatch.delenv("NFX_TET_KERNEL", raising=False)
+    cells = small_population()
+    meshes = [w.mesh() for w in cells]
+    b = Batch(0, tile_tets=128)
+    for w, m in zip(cells, meshes):
+        w.add_to_batch(b, m)
+    b.set_record(1, 50, 10)
+    b.finalize()
+    b.step(250)  # five captured 50-step graphs
+    b.record_now()
+    assert b.status() == 0
+    for i, (w, m) in enumerate(zip(cells, meshes)):
+        s = CellSim(0)
+        w.configure(s, m, max_rows=10)
+        s.step(250)
+        s.record_now()
+        assert np.array_equal(b.points(i), s.points()), i
+        assert np.array_equal(b.curve(i), s.curve()), i
+        s.close()
+    b.close()
+
+
+def test_batch_autotuned_matches_oracle():
+    cells = small_population()
+    b = Batch(0, tile_tets=0)
+    meshes = [w.mesh() for w in cells]
+    for w, m in zip(cells, meshes):
+        w.add_to_batch(b, m)
+    b.set_record(1, 50, 10)
+    b.finalize()
+    info = b.info()
+    assert info["tile_tets"] in (64, 128, 256)
+    assert [t for t, _ in info["tuning"]] == [64, 128, 256]
+    b.step(200)
+    b.record_now()
+    for i in (0, 3):
+        st = O.State(oracle_problem(cells[i], meshes[i]), "f64")
+        cref = st.run(200, 50)
+        assert rel_traj(st.positions(), b.points(i)) < 1e-5
+        assert rel_curve(cref, b.curve(i)) < 1e-4
+    b.close()
+
+
+def test_batch_rejects_mixed_models():
+    b = Batch(0, tile_tets=128)
+    w = Workload("x", radius=2.5, material="nh")
+    m = w.mesh()
+    c0 = b.add_cell(m.points, m.tets)
+    c1 = b.add_cell(m.points, m.tets)
+    b.set_tetra(c0, 0, 3e-3, 0.45, 1.0)
+    with pytest.raises(Exception):
+        b.set_viscoplastic(c1, (1e-3, 0, 1e-2, 1, 2e-4, 4e-3, 1, 0))
+    b.close()
