@@ -217,6 +217,56 @@ def run_reference(args):
 METRIC = "tetra-steps/s + % HBM peak, 1 GB300"
 
 
+def run_batched(args):
+    """Batched population (256 cells, radius log-uniform in [6, 40], per-cell materials): steps/s
+    of one batch advancing every cell, against looping the plain path over the same cells (each
+    cell's plain step time measured on that cell, summed). sims/s = cells / (20k steps' time)."""
+    from nofluidx3d_gb300.core import Batch, CellSim
+
+    cells = workloads.batched_cells(args.batch_cells, seed=0)
+    t0 = time.perf_counter()
+    meshes = [w.mesh() for w in cells]
+    t_mesh = time.perf_counter() - t0
+    nt = sum(m.num_tetra for m in meshes)
+    t0 = time.perf_counter()
+    b = Batch(0, tile_tets=args.batch_tile)
+    for w, m in zip(cells, meshes):
+        w.add_to_batch(b, m)
+    b.set_record(1, 100, args.warmup + args.steps + 10)
+    b.finalize()
+    t_setup = time.perf_counter() - t0
+    b.time_steps(args.warmup)
+    ms = b.time_steps(args.steps)
+    batch_step_ms = ms / args.steps
+    status = b.status()
+    info = b.info()
+    b.close()
+    # looped plain path: each cell alone, a short timed run per cell
+    plain_ms = []
+    for w, m in zip(cells, meshes):
+        s = CellSim(0)
+        w.configure(s, m, max_rows=4)
+        s.time_steps(10)
+        plain_ms.append(s.time_steps(args.loop_steps) / args.loop_steps)
+        s.close()
+    loop_step_ms = sum(plain_ms)
+    n = len(cells)
+    sim_steps = 20000
+    line = {
+        "metric": "batched sims/s (256 cells, 20k steps)", "value": n / (batch_step_ms * sim_steps / 1e3),
+        "unit": "sims/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": batch_step_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"batched {n} cells R~logU[6,40], per-cell VP materials", "tets": nt,
+                   "tile_tets": info["tile_tets"], "autotune_ms_per_10_steps": info["tuning"],
+                   "batch_tetra_steps_per_s": nt / (batch_step_ms / 1e3),
+                   "looped_plain_ms_per_step": loop_step_ms,
+                   "looped_plain_sims_per_s": n / (loop_step_ms * sim_steps / 1e3),
+                   "speedup_vs_looped_plain": loop_step_ms / batch_step_ms,
+                   "mesh_gen_s": t_mesh, "setup_s": t_setup, "status": status},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -229,11 +279,17 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--reference-seconds", type=float, default=90.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batched", action="store_true", help="batched population instead of one cell")
+    ap.add_argument("--batch-cells", type=int, default=256)
+    ap.add_argument("--batch-tile", type=int, default=0, help="0: autotune")
+    ap.add_argument("--loop-steps", type=int, default=50)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
         return run_reference(args)
+    if args.batched:
+        return run_batched(args)
 
     world, rank, local, dist = dist_setup()
     from nofluidx3d_gb300.core import CellSim
