@@ -263,23 +263,25 @@ int nfx_set_mesh(nfx_sim* s, int64_t np, int64_t nt, const double* points, const
     s->plan = std::move(plan);
     const MeshPlan& P = s->plan;
     auto& A = s->mesh_allocs;
-    int* tb; int* nbg; uint2* tn; uchar4* lc; ushort4* ti; float4 *da, *db; float2* dc; float4 *xh, *xl;
-    float4 *uh, *ul, *v, *fo; unsigned long long* fa; double* part;
-    const size_t ntp = (size_t)nt + ARRAY_PAD;  // per-tetra arrays carry ARRAY_PAD zeroed elements
+    int* tb; int* nbg; unsigned* tm; uint2* tn; uchar4* lc; ushort4* ti; float4 *da, *db; float2* dc;
+    float4 *xh, *xl, *uh, *ul, *v, *fo; unsigned long long* fa; double* part;
+    const int64_t ns = P.nslots;
+    const size_t ntp = (size_t)ns + ARRAY_PAD;  // per-slot arrays carry ARRAY_PAD zeroed elements
     if ((rc = dalloc(s, &tb, P.tile_tet_begin.size(), &A)) || (rc = dalloc(s, &nbg, P.tile_node_begin.size(), &A)) ||
+        (rc = dalloc(s, &tm, P.tile_meta.size(), &A)) ||
         (rc = dalloc(s, &tn, P.tile_nodes.size() / 2 + ARRAY_PAD, &A)) || (rc = dalloc(s, &lc, ntp, &A)) ||
         (rc = dalloc(s, &ti, ntp, &A)) ||
         (rc = dalloc(s, &da, ntp, &A)) || (rc = dalloc(s, &db, ntp, &A)) || (rc = dalloc(s, &dc, ntp, &A)) ||
         (rc = dalloc(s, &xh, (size_t)np, &A)) || (rc = dalloc(s, &xl, (size_t)np, &A)) || (rc = dalloc(s, &uh, (size_t)np, &A)) ||
         (rc = dalloc(s, &ul, (size_t)np, &A)) || (rc = dalloc(s, &v, (size_t)np, &A)) || (rc = dalloc(s, &fo, (size_t)np, &A)) ||
         (rc = dalloc(s, &fa, 3 * (size_t)np, &A)) || (rc = dalloc(s, &part, (size_t)((np + NODE_BLOCK - 1) / NODE_BLOCK), &A)) ||
-        (rc = dalloc(s, &s->d_node_user, (size_t)np, &A)) || (rc = dalloc(s, &s->d_stage, 9 * (size_t)std::max(np, nt), &A))) {
+        (rc = dalloc(s, &s->d_node_user, (size_t)np, &A)) || (rc = dalloc(s, &s->d_stage, 9 * (size_t)std::max(np, ns), &A))) {
         free_mesh(s);
         return rc;
     }
     // per-tetra constants, split into the float4/float4/float2 streams the kernel reads
-    std::vector<float> a(4 * (size_t)nt), b(4 * (size_t)nt), c(2 * (size_t)nt);
-    for (int64_t t = 0; t < nt; t++) {
+    std::vector<float> a(4 * (size_t)ns), b(4 * (size_t)ns), c(2 * (size_t)ns);
+    for (int64_t t = 0; t < ns; t++) {
         const float* o = &P.dmi[12 * t];
         for (int k = 0; k < 4; k++) a[4 * t + k] = o[k];
         for (int k = 0; k < 4; k++) b[4 * t + k] = o[4 + k];
@@ -298,6 +300,7 @@ int nfx_set_mesh(nfx_sim* s, int64_t np, int64_t nt, const double* points, const
     CUDA_TRY(cudaMemcpyAsync(tb, P.tile_tet_begin.data(), P.tile_tet_begin.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(nbg, P.tile_node_begin.data(), P.tile_node_begin.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(tn, P.tile_nodes.data(), P.tile_nodes.size() * sizeof(unsigned), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(tm, P.tile_meta.data(), P.tile_meta.size() * sizeof(unsigned), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(lc, P.lconn.data(), P.lconn.size(), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(ti, P.tile_inc.data(), P.tile_inc.size() * sizeof(uint16_t), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(da, a.data(), a.size() * sizeof(float), cudaMemcpyHostToDevice, st));
@@ -318,6 +321,7 @@ int nfx_set_mesh(nfx_sim* s, int64_t np, int64_t nt, const double* points, const
     s->mesh.tile_tet_begin = tb;
     s->mesh.tile_node_begin = nbg;
     s->mesh.tile_nodes = tn;
+    s->mesh.tile_meta = tm;
     s->mesh.lconn = lc;
     s->mesh.tile_inc = ti;
     s->mesh.dmi_a = da;
@@ -370,7 +374,7 @@ int nfx_set_viscoplastic(nfx_sim* s, const double* par) {
     CHECK_ARG(par[6] != 0, "hardening threshold must be non-zero");
     int rc;
     if ((rc = set_device(s)) != NFX_OK) return rc;
-    const size_t ntp = (size_t)s->plan.nt + ARRAY_PAD;
+    const size_t ntp = (size_t)s->plan.nslots + ARRAY_PAD;
     if (!s->st.vp_a) {
         if ((rc = dalloc(s, &s->st.vp_a, ntp, &s->mesh_allocs)) || (rc = dalloc(s, &s->st.vp_b, ntp, &s->mesh_allocs)) ||
             (rc = dalloc(s, &s->st.vp_c, ntp, &s->mesh_allocs)) || (rc = dalloc(s, &s->st.fields, ntp, &s->mesh_allocs)))
@@ -585,7 +589,7 @@ int nfx_get_tet_field(nfx_sim* s, int which, double* out) {
     CHECK_ARG(s && out, "null argument");
     CHECK_ARG(which >= 0 && which <= 2, "unknown field");
     if (!s->have_mesh) return fail(NFX_ERR_STATE, "no mesh");
-    const int64_t nt = s->plan.nt;
+    const int64_t nt = s->plan.nt, ns = s->plan.nslots;
     if (s->mat.model != MODEL_VP || !s->st.vp_c) {
         // the elastic kernel (tetra.cl) writes no per-tetra fields; the reference's buffers stay 0
         std::fill(out, out + nt, 0.0);
@@ -593,12 +597,13 @@ int nfx_get_tet_field(nfx_sim* s, int which, double* out) {
     }
     int rc;
     if ((rc = set_device(s)) != NFX_OK) return rc;
-    std::vector<float> h(2 * (size_t)nt);
+    std::vector<float> h(2 * (size_t)ns);
     const float2* src = which == 2 ? s->st.vp_c : s->st.fields;
-    CUDA_TRY(cudaMemcpyAsync(h.data(), src, (size_t)nt * sizeof(float2), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaMemcpyAsync(h.data(), src, (size_t)ns * sizeof(float2), cudaMemcpyDeviceToHost, s->stream));
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     const int comp = which == 0 ? 0 : 1;
-    for (int64_t t = 0; t < nt; t++) out[s->plan.tet_user[t]] = (double)h[2 * t + comp];
+    for (int64_t t = 0; t < ns; t++)
+        if (s->plan.tet_user[t] >= 0) out[s->plan.tet_user[t]] = (double)h[2 * t + comp];
     return NFX_OK;
 }
 
@@ -613,13 +618,15 @@ int nfx_get_plastic_tensor(nfx_sim* s, double* out) {
     }
     int rc;
     if ((rc = set_device(s)) != NFX_OK) return rc;
-    std::vector<float> a(4 * (size_t)nt), b(4 * (size_t)nt), c(2 * (size_t)nt);
-    CUDA_TRY(cudaMemcpyAsync(a.data(), s->st.vp_a, (size_t)nt * sizeof(float4), cudaMemcpyDeviceToHost, s->stream));
-    CUDA_TRY(cudaMemcpyAsync(b.data(), s->st.vp_b, (size_t)nt * sizeof(float4), cudaMemcpyDeviceToHost, s->stream));
-    CUDA_TRY(cudaMemcpyAsync(c.data(), s->st.vp_c, (size_t)nt * sizeof(float2), cudaMemcpyDeviceToHost, s->stream));
+    const int64_t ns = s->plan.nslots;
+    std::vector<float> a(4 * (size_t)ns), b(4 * (size_t)ns), c(2 * (size_t)ns);
+    CUDA_TRY(cudaMemcpyAsync(a.data(), s->st.vp_a, (size_t)ns * sizeof(float4), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaMemcpyAsync(b.data(), s->st.vp_b, (size_t)ns * sizeof(float4), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaMemcpyAsync(c.data(), s->st.vp_c, (size_t)ns * sizeof(float2), cudaMemcpyDeviceToHost, s->stream));
     CUDA_TRY(cudaStreamSynchronize(s->stream));
-    for (int64_t t = 0; t < nt; t++) {
+    for (int64_t t = 0; t < ns; t++) {
         const int64_t u = s->plan.tet_user[t];
+        if (u < 0) continue;  // padding slot
         const float P[9] = {a[4 * t], a[4 * t + 1], a[4 * t + 2], a[4 * t + 3], b[4 * t], b[4 * t + 1],
                             b[4 * t + 2], b[4 * t + 3], c[2 * t]};
         for (int k = 0; k < 9; k++) out[k * nt + u] = (double)P[k] + ((k % 4 == 0) ? 1.0 : 0.0);
@@ -727,7 +734,9 @@ int nfx_mesh_info(nfx_sim* s, int64_t* ntiles, int64_t* tile_nodes) {
     CHECK_ARG(s && ntiles && tile_nodes, "null argument");
     if (!s->have_mesh) return fail(NFX_ERR_STATE, "no mesh");
     *ntiles = s->plan.ntiles;
-    *tile_nodes = (int64_t)s->plan.tile_nodes.size() / 2;
+    int64_t nodes = 0;
+    for (uint32_t m : s->plan.tile_meta) nodes += m >> 16;
+    *tile_nodes = nodes;
     return NFX_OK;
 }
 

@@ -139,7 +139,7 @@ int build_device(nfx_batch* b, const std::vector<int>& which, int tile_tets, Bat
         c.block_base = nblocks;
         c.nblocks = (c.np + NODE_BLOCK - 1) / NODE_BLOCK;
         np += c.nblocks * NODE_BLOCK;  // whole blocks per cell
-        nt += c.nt;
+        nt += c.plan.nslots;  // tetra slots (whole tiles)
         ntiles += c.plan.ntiles;
         nblocks += c.nblocks;
         ntn += (int64_t)c.plan.tile_nodes.size() / 2;
@@ -147,6 +147,7 @@ int build_device(nfx_batch* b, const std::vector<int>& which, int tile_tets, Bat
     if (np > 0x7fffffff || nt > 0x7fffffff) return bfail(NFX_ERR_ARG, "batch too large");
     const size_t ntp = (size_t)nt + ARRAY_PAD;
     std::vector<int> tile_tet_begin(ntiles + 1), tile_node_begin(ntiles + 1), tile_cell(ntiles), block_cell(nblocks);
+    std::vector<unsigned> tile_meta(ntiles);
     std::vector<uint32_t> tile_nodes(2 * (size_t)ntn);
     std::vector<uint8_t> lconn(4 * ntp, 0);
     std::vector<uint16_t> tile_inc(4 * ntp, 0);
@@ -160,6 +161,7 @@ int build_device(nfx_batch* b, const std::vector<int>& which, int tile_tets, Bat
         for (int64_t t = 0; t < P.ntiles; t++) {
             tile_tet_begin[c.tile_base + t] = (int)(c.tet_base + P.tile_tet_begin[t]);
             tile_node_begin[c.tile_base + t] = (int)(tn_pos + P.tile_node_begin[t]);
+            tile_meta[c.tile_base + t] = P.tile_meta[t];
             tile_cell[c.tile_base + t] = (int)k;
         }
         for (size_t q = 0; q < P.tile_nodes.size() / 2; q++) {
@@ -169,7 +171,7 @@ int build_device(nfx_batch* b, const std::vector<int>& which, int tile_tets, Bat
         tn_pos += (int64_t)P.tile_nodes.size() / 2;
         std::memcpy(&lconn[4 * c.tet_base], P.lconn.data(), P.lconn.size());
         std::memcpy(&tile_inc[4 * c.tet_base], P.tile_inc.data(), P.tile_inc.size() * sizeof(uint16_t));
-        for (int64_t t = 0; t < c.nt; t++) {
+        for (int64_t t = 0; t < P.nslots; t++) {
             const float* o = &P.dmi[12 * t];
             const size_t g = (size_t)(c.tet_base + t);
             for (int q = 0; q < 4; q++) da[4 * g + q] = o[q];
@@ -207,14 +209,14 @@ int build_device(nfx_batch* b, const std::vector<int>& which, int tile_tets, Bat
     tile_node_begin[ntiles] = (int)tn_pos;
 
     auto& A = D.allocs;
-    int* d_ttb; int* d_tnb; uint2* d_tn; uchar4* d_lc; ushort4* d_ti; float4 *d_da, *d_db; float2* d_dc;
+    int* d_ttb; int* d_tnb; unsigned* d_tm; uint2* d_tn; uchar4* d_lc; ushort4* d_ti; float4 *d_da, *d_db; float2* d_dc;
     float4 *d_xh, *d_xl, *d_uh, *d_ul, *d_v, *d_fo; unsigned long long* d_fa; double* d_part;
     CellDev* d_cells; int *d_tc, *d_bc; unsigned* d_cc; double* d_curves = nullptr;
     float4 *d_pa = nullptr, *d_pb = nullptr; float2 *d_pc = nullptr, *d_fields = nullptr;
     int rc;
     const size_t rows = (size_t)std::max<long long>(b->max_rows, 1);
     if ((rc = balloc(A, &d_ttb, ntiles + 1)) || (rc = balloc(A, &d_tnb, ntiles + 1)) ||
-        (rc = balloc(A, &d_tn, ntn + ARRAY_PAD)) || (rc = balloc(A, &d_lc, ntp)) || (rc = balloc(A, &d_ti, ntp)) ||
+        (rc = balloc(A, &d_tm, ntiles)) || (rc = balloc(A, &d_tn, ntn + ARRAY_PAD)) || (rc = balloc(A, &d_lc, ntp)) || (rc = balloc(A, &d_ti, ntp)) ||
         (rc = balloc(A, &d_da, ntp)) || (rc = balloc(A, &d_db, ntp)) || (rc = balloc(A, &d_dc, ntp)) ||
         (rc = balloc(A, &d_xh, np)) || (rc = balloc(A, &d_xl, np)) || (rc = balloc(A, &d_uh, np)) ||
         (rc = balloc(A, &d_ul, np)) || (rc = balloc(A, &d_v, np)) || (rc = balloc(A, &d_fo, np)) ||
@@ -232,6 +234,7 @@ int build_device(nfx_batch* b, const std::vector<int>& which, int tile_tets, Bat
     BCUDA(cudaMemcpyAsync(d_ttb, tile_tet_begin.data(), tile_tet_begin.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     BCUDA(cudaMemcpyAsync(d_tnb, tile_node_begin.data(), tile_node_begin.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     BCUDA(cudaMemsetAsync(d_tn, 0, (ntn + ARRAY_PAD) * sizeof(uint2), st));
+    BCUDA(cudaMemcpyAsync(d_tm, tile_meta.data(), tile_meta.size() * sizeof(unsigned), cudaMemcpyHostToDevice, st));
     BCUDA(cudaMemcpyAsync(d_tn, tile_nodes.data(), tile_nodes.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
     BCUDA(cudaMemcpyAsync(d_lc, lconn.data(), lconn.size(), cudaMemcpyHostToDevice, st));
     BCUDA(cudaMemcpyAsync(d_ti, tile_inc.data(), tile_inc.size() * sizeof(uint16_t), cudaMemcpyHostToDevice, st));
@@ -264,6 +267,7 @@ int build_device(nfx_batch* b, const std::vector<int>& which, int tile_tets, Bat
     M.tile_tet_begin = d_ttb;
     M.tile_node_begin = d_tnb;
     M.tile_nodes = d_tn;
+    M.tile_meta = d_tm;
     M.lconn = d_lc;
     M.tile_inc = d_ti;
     M.dmi_a = d_da;

@@ -41,20 +41,25 @@ constexpr int ARRAY_PAD = 16;
 // ---------------------------------------------------------------------------------------
 // Host-side mesh plan: reordering, tiles, per-tetra reference quantities.
 // ---------------------------------------------------------------------------------------
+// Tiles sit at a fixed stride: tile b owns tetra slots [b*T, (b+1)*T) and node-list entries
+// [b*NMAX, (b+1)*NMAX), NMAX = min(T, 256); slots and entries past the tile's real counts
+// (tile_meta) are zero padding.
 struct MeshPlan {
     int64_t np = 0, nt = 0, ntiles = 0;
-    int tile_tets = TILE_TETS;
+    int64_t nslots = 0;                    // ntiles * tile_tets
+    int tile_tets = DEFAULT_TILE_TETS;
     std::vector<int64_t> node_user;   // internal node -> user node id
     std::vector<int64_t> node_int;    // user node id -> internal node
-    std::vector<int64_t> tet_user;    // internal tetra -> user tetra id
-    std::vector<int32_t> tile_tet_begin;   // ntiles + 1
-    std::vector<int32_t> tile_node_begin;  // ntiles + 1
-    std::vector<uint32_t> tile_nodes;      // 2 per tile node: internal node id, (first << 16 | count)
+    std::vector<int64_t> tet_user;    // tetra slot -> user tetra id, -1 for padding
+    std::vector<int32_t> tile_tet_begin;   // ntiles + 1 (= b*T)
+    std::vector<int32_t> tile_node_begin;  // ntiles + 1 (= b*NMAX)
+    std::vector<uint32_t> tile_meta;       // per tile: tetra count | node count << 16
+    std::vector<uint32_t> tile_nodes;      // 2 per node entry: internal node id, (first << 16 | count)
                                            // of its run in the tile's incidence list
-    std::vector<uint8_t> lconn;            // 4 * nt local corner indices (internal tet order)
-    std::vector<uint16_t> tile_inc;        // 4 * nt: per tile, the corners (4*local tet + corner)
+    std::vector<uint8_t> lconn;            // 4 * nslots local corner indices
+    std::vector<uint16_t> tile_inc;        // 4 * nslots: per tile, the corners (4*local tet + corner)
                                            // grouped by local node in node order, tet order within
-    std::vector<float> dmi;                // 12 * nt: Dm^-1 row-major (9), V0, pad, pad
+    std::vector<float> dmi;                // 12 * nslots: Dm^-1 row-major (9), V0, pad, pad
     std::vector<float> Xh, Xl;             // 4 * np: reference position hi / lo parts
 };
 
@@ -71,6 +76,7 @@ struct MeshDev {
     int tile_tets;
     const int* tile_tet_begin;
     const int* tile_node_begin;
+    const unsigned* tile_meta; // tetra count | node count << 16
     const uint2* tile_nodes;   // (node id, first << 16 | count)
     const uchar4* lconn;
     const ushort4* tile_inc;   // four incidence entries per tetra slot of the tile

@@ -139,35 +139,33 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * 64))
 
     const int b = blockIdx.x;
     const int j = threadIdx.x;
-    const int tb = m.tile_tet_begin[b];
-    const int ntt = m.tile_tet_begin[b + 1] - tb;
-    const int nb = m.tile_node_begin[b];
-    const int nn = m.tile_node_begin[b + 1] - nb;
+    // fixed-stride tiles: the tile's slots and node entries are addressed without a load; the
+    // real counts come from the tile's meta word (loaded alongside the data)
+    const int t = b * TILE + j;
+    const int nb = b * NMAX;
+    const unsigned meta = __ldg(m.tile_meta + b);
+    const int ntt = (int)(meta & 0xffffu);
+    const int nn = (int)(meta >> 16);
     const bool act = j < ntt;
-    const int t = tb + j;
     const bool wf = fields_due(s, fields_every, t_offset);
 
-    // streaming per-tetra data first (read once per step: evict-first)
-    uchar4 lc = make_uchar4(0, 0, 0, 0);
-    float4 da = make_float4(0.f, 0.f, 0.f, 0.f), db = da;
-    float2 dc = make_float2(0.f, 0.f);
-    float4 pa = da, pb = da;
-    float2 pc = dc;
-    if (act) {
-        lc = __ldcs(m.lconn + t);
-        da = __ldcs(m.dmi_a + t);
-        db = __ldcs(m.dmi_b + t);
-        dc = __ldcs(m.dmi_c + t);
-        if (MODEL == MODEL_VP) {
-            pa = __ldcs(s.vp_a + t);
-            pb = __ldcs(s.vp_b + t);
-            pc = __ldcs(s.vp_c + t);
-        }
-        s_inc[j] = __ldcs(m.tile_inc + t);
+    // Streaming per-tetra data (read once per step: evict-first) and the node list, issued for
+    // every slot and entry without waiting for the meta word: padding is valid zeroed memory.
+    const uchar4 lc = __ldcs(m.lconn + t);
+    const float4 da = __ldcs(m.dmi_a + t);
+    const float4 db = __ldcs(m.dmi_b + t);
+    const float2 dc = __ldcs(m.dmi_c + t);
+    float4 pa = make_float4(0.f, 0.f, 0.f, 0.f), pb = pa;
+    float2 pc = make_float2(0.f, 0.f);
+    if (MODEL == MODEL_VP) {
+        pa = __ldcs(s.vp_a + t);
+        pb = __ldcs(s.vp_b + t);
+        pc = __ldcs(s.vp_c + t);
     }
+    s_inc[j] = __ldcs(m.tile_inc + t);
     uint2 node = make_uint2(0u, 0u);
-    if (j < nn) {
-        node = m.tile_nodes[nb + j];
+    if (j < NMAX) {
+        node = __ldcs(m.tile_nodes + nb + j);
         s_uh[j] = s.uh[node.x];
         s_ul[j] = s.ul[node.x];
     }

@@ -121,25 +121,25 @@ bool build_mesh_plan(int64_t np, int64_t nt, const double* P, const uint32_t* T,
         }
         tkey[t] = morton3(Q.q(c[0], 0), Q.q(c[1], 1), Q.q(c[2], 2));
     }
-    plan.tet_user.resize(nt);
-    std::iota(plan.tet_user.begin(), plan.tet_user.end(), 0);
-    std::stable_sort(plan.tet_user.begin(), plan.tet_user.end(),
-                     [&](int64_t a, int64_t b) { return tkey[a] < tkey[b]; });
+    std::vector<int64_t> order(nt);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return tkey[a] < tkey[b]; });
 
-    // tiles
-    plan.lconn.resize(4 * (size_t)nt);
-    plan.tile_inc.resize(4 * (size_t)nt);
-    plan.tile_tet_begin.push_back(0);
-    plan.tile_node_begin.push_back(0);
+    // Tiles at a fixed stride: tile b owns tetra slots [b*T, b*T + T) and node-list entries
+    // [b*NMAX, b*NMAX + NMAX); unused slots and entries are zero padding (a padding tetra has
+    // Dm^-1 = 0 and V0 = 0 and produces no force; a padding node entry has count 0). Kernels can
+    // then address a tile's data without first loading its offsets.
+    const int64_t T_ = tile_tets, NM_ = nodes_max;
+    std::vector<int64_t> slot_user;  // tetra slot -> user tetra (-1: padding)
     std::vector<uint32_t> ids;
     ids.reserve(4 * (size_t)tile_tets);
-    int64_t t0 = 0;
+    int64_t t0 = 0, b = 0;
     while (t0 < nt) {
         int64_t cnt = std::min<int64_t>(tile_tets, nt - t0);
         for (;;) {
             ids.clear();
             for (int64_t j = 0; j < cnt; j++) {
-                const int64_t ut = plan.tet_user[t0 + j];
+                const int64_t ut = order[t0 + j];
                 for (int k = 0; k < 4; k++) ids.push_back((uint32_t)plan.node_int[T[k * nt + ut]]);
             }
             std::sort(ids.begin(), ids.end());
@@ -148,13 +148,18 @@ bool build_mesh_plan(int64_t np, int64_t nt, const double* P, const uint32_t* T,
             cnt = std::max<int64_t>(1, cnt - 16);
         }
         const size_t nn = ids.size();
+        const size_t s0 = (size_t)(b * T_);
+        slot_user.resize(s0 + T_, -1);
+        plan.lconn.resize(4 * (s0 + T_), 0);
+        plan.tile_inc.resize(4 * (s0 + T_), 0);
         std::vector<uint32_t> count(nn, 0), first(nn, 0);
         for (int64_t j = 0; j < cnt; j++) {
-            const int64_t ut = plan.tet_user[t0 + j];
+            const int64_t ut = order[t0 + j];
+            slot_user[s0 + j] = ut;
             for (int k = 0; k < 4; k++) {
                 const uint32_t g = (uint32_t)plan.node_int[T[k * nt + ut]];
                 const size_t loc = std::lower_bound(ids.begin(), ids.end(), g) - ids.begin();
-                plan.lconn[4 * (t0 + j) + k] = (uint8_t)loc;
+                plan.lconn[4 * (s0 + j) + k] = (uint8_t)loc;
                 count[loc]++;
             }
         }
@@ -163,23 +168,33 @@ bool build_mesh_plan(int64_t np, int64_t nt, const double* P, const uint32_t* T,
         std::vector<uint32_t> fill(first);
         for (int64_t j = 0; j < cnt; j++)
             for (int k = 0; k < 4; k++) {
-                const uint8_t loc = plan.lconn[4 * (t0 + j) + k];
-                plan.tile_inc[4 * t0 + fill[loc]++] = (uint16_t)(4 * j + k);
+                const uint8_t loc = plan.lconn[4 * (s0 + j) + k];
+                plan.tile_inc[4 * s0 + fill[loc]++] = (uint16_t)(4 * j + k);
             }
+        plan.tile_nodes.resize(2 * (size_t)((b + 1) * NM_), 0u);
         for (size_t q = 0; q < nn; q++) {
-            plan.tile_nodes.push_back(ids[q]);
-            plan.tile_nodes.push_back((first[q] << 16) | count[q]);
+            plan.tile_nodes[2 * (b * NM_ + q)] = ids[q];
+            plan.tile_nodes[2 * (b * NM_ + q) + 1] = (first[q] << 16) | count[q];
         }
+        plan.tile_meta.push_back((uint32_t)cnt | ((uint32_t)nn << 16));
         t0 += cnt;
-        plan.tile_tet_begin.push_back((int32_t)t0);
-        plan.tile_node_begin.push_back((int32_t)(plan.tile_nodes.size() / 2));
+        b++;
     }
-    plan.ntiles = (int64_t)plan.tile_tet_begin.size() - 1;
+    plan.ntiles = b;
+    plan.nslots = b * T_;
+    plan.tet_user = std::move(slot_user);
+    plan.tile_tet_begin.resize(b + 1);
+    plan.tile_node_begin.resize(b + 1);
+    for (int64_t q = 0; q <= b; q++) {
+        plan.tile_tet_begin[q] = (int32_t)(q * T_);
+        plan.tile_node_begin[q] = (int32_t)(q * NM_);
+    }
 
-    // per-tetra Dm^-1 and V0 (internal order)
-    plan.dmi.assign(12 * (size_t)nt, 0.0f);
-    for (int64_t it = 0; it < nt; it++) {
+    // per-tetra Dm^-1 and V0 (slot order; padding slots stay zero)
+    plan.dmi.assign(12 * (size_t)plan.nslots, 0.0f);
+    for (int64_t it = 0; it < plan.nslots; it++) {
         const int64_t ut = plan.tet_user[it];
+        if (ut < 0) continue;
         const int64_t n0 = T[ut];
         double M[9];  // columns X_k - X_0
         for (int k = 0; k < 3; k++) {
