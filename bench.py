@@ -325,7 +325,7 @@ def main():
 
     pos_host = torch.empty(3 * npn, dtype=torch.float64, pin_memory=True).numpy()
     tab_host = torch.empty(w.record_every, dtype=torch.float64, pin_memory=True).numpy()
-    c = w.contacts()[w.record_contact]
+    c = w.contacts(mesh)[w.record_contact]
     intervals = max(1, args.e2e_steps // w.record_every)
     barrier(dist, local)
     sim.sync()

@@ -209,6 +209,9 @@ int nfx_batch_step(nfx_batch* batch, int64_t nsteps);
 int nfx_batch_time_steps(nfx_batch* batch, int64_t nsteps, float* ms);
 /* Records the row of the current time for every cell (see nfx_record_now). */
 int nfx_batch_record_now(nfx_batch* batch);
+/* On-demand indenter force of contact index `contact` of every cell (Simulation.py:142-157,
+ * evaluated per cell), out = double[cells]; a cell with fewer contacts reads 0. */
+int nfx_batch_indenter_force(nfx_batch* batch, int contact, double* out);
 /* Force curve of one cell (rows of t, indentation, force); *n_rows = rows available. */
 int nfx_batch_get_curve(nfx_batch* batch, int cell, double* rows, int64_t max_rows, int64_t* n_rows);
 /* Node positions of one cell, double[3*np] SoA in the cell's user order. */

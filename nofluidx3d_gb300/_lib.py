@@ -81,6 +81,7 @@ _SIGS = {
     "nfx_batch_step": ([_vp, _i64], C.c_int),
     "nfx_batch_time_steps": ([_vp, _i64, C.POINTER(C.c_float)], C.c_int),
     "nfx_batch_record_now": ([_vp], C.c_int),
+    "nfx_batch_indenter_force": ([_vp, C.c_int, _vp], C.c_int),
     "nfx_batch_get_curve": ([_vp, C.c_int, _vp, _i64, C.POINTER(_i64)], C.c_int),
     "nfx_batch_get_points": ([_vp, C.c_int, _vp], C.c_int),
     "nfx_batch_status": ([_vp, C.POINTER(C.c_uint32), C.c_int], C.c_int),

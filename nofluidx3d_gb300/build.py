@@ -47,13 +47,23 @@ def up_to_date() -> bool:
     return all(p.stat().st_mtime <= t for p in _inputs())
 
 
+def tuning_defines() -> list[str]:
+    """Kernel tuning macros from NFX_NVCC_DEFINES (space-separated -DNAME=VALUE, e.g.
+    -DNFX_NODE_MIN_BLOCKS=4); anything that is not a -D flag is rejected."""
+    flags = os.environ.get("NFX_NVCC_DEFINES", "").split()
+    for f in flags:
+        if not f.startswith("-D") or len(f) < 3:
+            raise ValueError(f"NFX_NVCC_DEFINES takes -DNAME[=VALUE] flags only, got {f!r}")
+    return flags
+
+
 def build(force: bool = False, verbose: bool = False) -> Path:
     """Compile and link libnfx.so unless it is newer than every source. Returns its path."""
     if not force and up_to_date():
         return lib_path()
     nvcc = nvcc_path()
     BUILD_DIR.mkdir(exist_ok=True)
-    common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", f"-I{INCLUDE}", f"-I{CSRC}"]
+    common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", f"-I{INCLUDE}", f"-I{CSRC}", *tuning_defines()]
     procs = []
     objs = []
     for src in SOURCES:

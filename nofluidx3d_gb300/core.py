@@ -270,6 +270,12 @@ class Batch:
     def record_now(self) -> None:
         check(self._L.nfx_batch_record_now(self._h))
 
+    def indenter_force(self, contact: int) -> np.ndarray:
+        """Current force on contact index `contact` of every cell (0 where a cell has fewer)."""
+        out = np.zeros(len(self.cells), np.float64)
+        check(self._L.nfx_batch_indenter_force(self._h, int(contact), _ptr(out)))
+        return out
+
     def curve(self, cell: int) -> np.ndarray:
         n = C.c_int64()
         check(self._L.nfx_batch_get_curve(self._h, int(cell), None, 0, C.byref(n)))

@@ -51,8 +51,13 @@ struct nfx_sim {
     std::vector<void*> mesh_allocs;  // freed on re-mesh
     MeshDev mesh{};
     StateDev st{};
-    MaterialDev mat{};
-    StepParams prm{};
+    // The simulation's parameters: a one-cell table the kernels read from device memory. The
+    // host copy is uploaded in stream order before the next launch after any change.
+    CellDev cell{};
+    CellDev* d_cell = nullptr;
+    bool cell_dirty = true;
+    int nblocks = 0;                 // node blocks
+    long long record_every = 0, max_rows = 0, fields_every = 0;
     long long* d_node_user = nullptr;
     double* d_stage = nullptr;
     double* d_tables[MAX_CONTACTS] = {nullptr, nullptr, nullptr, nullptr};
@@ -100,12 +105,22 @@ void free_mesh(nfx_sim* s) {
     s->st = StateDev{};
     s->st.status = keep.status;
     s->st.time = keep.time;
-    s->st.counter = keep.counter;
     s->st.force_out = keep.force_out;
-    s->st.curve = keep.curve;
     s->d_node_user = nullptr;
     s->d_stage = nullptr;
     s->have_mesh = false;
+}
+
+// Kernel view of the one-cell table (no tile or block maps: everything is cell 0).
+BatchDev table_view(const nfx_sim* s) {
+    BatchDev b{};
+    b.cells = s->d_cell;
+    b.cell_counter = s->d_counter;
+    b.curves = s->d_curve;
+    b.record_every = s->record_every;
+    b.max_rows = s->max_rows;
+    b.fields_every = s->fields_every;
+    return b;
 }
 
 void invalidate_graph(nfx_sim* s) {
@@ -121,25 +136,39 @@ int require_ready(nfx_sim* s) {
     return NFX_OK;
 }
 
+// Upload the parameter table if it changed (stream-ordered: launches already enqueued read the
+// old values, later ones the new). Pageable source: the copy has taken the bytes on return.
+int upload_cell(nfx_sim* s) {
+    if (!s->cell_dirty) return NFX_OK;
+    CUDA_TRY(cudaMemcpyAsync(s->d_cell, &s->cell, sizeof(CellDev), cudaMemcpyHostToDevice, s->stream));
+    s->cell_dirty = false;
+    return NFX_OK;
+}
+
 // Element pass launch: the one-CTA-per-tile kernel by default. NFX_TET_KERNEL=1 in the
 // environment selects the persistent pipelined kernel (tiles of at most 256) on a grid of
 // (resident CTAs per SM) x (SM count), capped at the tile count.
 cudaError_t launch_elem(nfx_sim* s, int k) {
     if (s->tet_variant == 1 && s->mesh.tile_tets <= TILE_TETS) {
-        int& bps = s->pipe_bps[s->mat.model & 3];
-        if (bps < 0) bps = pipe_blocks_per_sm(s->mat.model, s->mesh.tile_tets);
+        const int model = s->cell.mat.model;
+        int& bps = s->pipe_bps[model & 3];
+        if (bps < 0) bps = pipe_blocks_per_sm(model, s->mesh.tile_tets);
         if (bps > 0) {
             const long long grid = std::min<long long>((long long)bps * s->sm_count, s->mesh.ntiles);
-            return launch_tet_pass_pipe(s->mesh, s->st, s->mat, s->prm, k, (int)grid, s->stream);
+            return launch_tet_pass_pipe(s->mesh, s->st, table_view(s), model, k, (int)grid, s->stream);
         }
     }
-    return launch_tet_pass(s->mesh, s->st, s->mat, s->prm, k, s->stream);
+    return launch_tet_pass(s->mesh, s->st, table_view(s), s->cell.mat.model, k, s->stream);
+}
+
+cudaError_t launch_nodes(nfx_sim* s, int k, int mode, int readout_contact) {
+    return launch_node_pass(s->mesh, s->st, table_view(s), s->nblocks, k, mode, readout_contact, s->stream);
 }
 
 int enqueue_steps(nfx_sim* s, int n) {
     for (int k = 0; k < n; k++) {
         CUDA_TRY(launch_elem(s, k));
-        CUDA_TRY(launch_node_pass(s->mesh, s->st, s->prm, k, NODE_UPDATE, -1, s->stream));
+        CUDA_TRY(launch_nodes(s, k, NODE_UPDATE, -1));
     }
     CUDA_TRY(launch_advance_time(s->st, n, s->stream));
     return NFX_OK;
@@ -163,10 +192,19 @@ int build_graph(nfx_sim* s) {
     return NFX_OK;
 }
 
+// A new material: the captured graph holds the kernel of one material model, so it is rebuilt only
+// when the model changes; parameters travel through the table.
+void set_material(nfx_sim* s, const MaterialDev& m) {
+    if (!s->have_material || s->cell.mat.model != m.model) invalidate_graph(s);
+    s->cell.mat = m;
+    s->cell_dirty = true;
+    s->have_material = true;
+}
+
 void note_rows(nfx_sim* s, long long t_begin, long long t_end_inclusive) {
     // rows produced by node passes at times in [t_begin, t_end_inclusive]
-    const long long every = s->prm.record_every;
-    if (s->prm.record_contact < 0 || every <= 0 || t_end_inclusive < t_begin) return;
+    const long long every = s->record_every;
+    if (s->cell.record_contact < 0 || every <= 0 || t_end_inclusive < t_begin) return;
     const long long last = t_end_inclusive / every;  // last row index touched
     if (last * every >= t_begin) s->rows_written = std::max(s->rows_written, std::min(last + 1, s->curve_rows));
 }
@@ -200,7 +238,8 @@ int nfx_create(int device, nfx_sim** out) {
     e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { delete s; return fail(NFX_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)); }
     if ((rc = dalloc(s, &s->d_status, 1, nullptr)) != NFX_OK || (rc = dalloc(s, &s->d_time, 1, nullptr)) != NFX_OK ||
-        (rc = dalloc(s, &s->d_counter, 1, nullptr)) != NFX_OK || (rc = dalloc(s, &s->d_force_out, 1, nullptr)) != NFX_OK) {
+        (rc = dalloc(s, &s->d_counter, 1, nullptr)) != NFX_OK || (rc = dalloc(s, &s->d_force_out, 1, nullptr)) != NFX_OK ||
+        (rc = dalloc(s, &s->d_cell, 1, nullptr)) != NFX_OK) {
         nfx_destroy(s);
         return rc;
     }
@@ -209,10 +248,9 @@ int nfx_create(int device, nfx_sim** out) {
     cudaMemsetAsync(s->d_counter, 0, sizeof(unsigned), s->stream);
     s->st.status = s->d_status;
     s->st.time = s->d_time;
-    s->st.counter = s->d_counter;
     s->st.force_out = s->d_force_out;
-    s->prm.record_contact = -1;
-    s->prm.fix_a = s->prm.fix_b = -1;
+    s->cell.record_contact = -1;
+    s->cell.fix_a = s->cell.fix_b = -1;
     cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, device);
     if (s->sm_count < 1) s->sm_count = 1;
     if (const char* v = std::getenv("NFX_TET_KERNEL")) s->tet_variant = std::atoi(v) == 1 ? 1 : 0;
@@ -222,9 +260,9 @@ int nfx_create(int device, nfx_sim** out) {
     }
     // default integrator: the reference's xi = 0.005 (VelocityVerlet.cl:11)
     const double xi = 0.005;
-    s->prm.vv_a = (float)((1 - 0.5 * xi) / (1 + 0.5 * xi));
-    s->prm.vv_hb = (float)(0.5 / (1 + 0.5 * xi));
-    s->prm.vv_dm = (float)(1 - 0.5 * xi);
+    s->cell.vv_a = (float)((1 - 0.5 * xi) / (1 + 0.5 * xi));
+    s->cell.vv_hb = (float)(0.5 / (1 + 0.5 * xi));
+    s->cell.vv_dm = (float)(1 - 0.5 * xi);
     *out = s;
     return NFX_OK;
 }
@@ -244,6 +282,7 @@ int nfx_destroy(nfx_sim* s) {
     if (s->d_time) cudaFree(s->d_time);
     if (s->d_counter) cudaFree(s->d_counter);
     if (s->d_force_out) cudaFree(s->d_force_out);
+    if (s->d_cell) cudaFree(s->d_cell);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return NFX_OK;
@@ -337,10 +376,16 @@ int nfx_set_mesh(nfx_sim* s, int64_t np, int64_t nt, const double* points, const
     s->st.partials = part;
     s->time = 0;
     s->rows_written = 0;
-    s->prm.fix_a = s->prm.fix_b = -1;
+    s->nblocks = (int)((np + NODE_BLOCK - 1) / NODE_BLOCK);
+    s->cell.fix_a = s->cell.fix_b = -1;
+    s->cell.node_begin = 0;
+    s->cell.node_end = (int)np;
+    s->cell.block_begin = 0;
+    s->cell.block_end = s->nblocks;
+    s->cell_dirty = true;
     s->have_mesh = true;
     // the viscoplastic state follows the mesh
-    if (s->have_material && s->mat.model == MODEL_VP) {
+    if (s->have_material && s->cell.mat.model == MODEL_VP) {
         s->have_material = false;
         return fail(NFX_ERR_STATE, "mesh replaced: call nfx_set_viscoplastic again");
     }
@@ -354,15 +399,14 @@ int nfx_set_tetra(nfx_sim* s, int model, double E, double nu, double mr) {
     CHECK_ARG(nu != 0.5, "poisson ratio 0.5 makes the bulk modulus infinite");
     // constants of tetra.cl:79-84, :97-102, :118-121
     const double mu = E / (2 * (1 + nu));
-    s->mat = MaterialDev{};
-    s->mat.model = model;
-    s->mat.mu1 = (float)(mr * mu);
-    s->mat.mu2 = (float)((1 - mr) * mu);
-    s->mat.kappa = (float)(E / (3 * (1 - 2 * nu)));
-    s->mat.mu = (float)mu;
-    s->mat.kp = (float)(nu / (1 - 2 * nu));
-    s->have_material = true;
-    invalidate_graph(s);
+    MaterialDev m{};
+    m.model = model;
+    m.mu1 = (float)(mr * mu);
+    m.mu2 = (float)((1 - mr) * mu);
+    m.kappa = (float)(E / (3 * (1 - 2 * nu)));
+    m.mu = (float)mu;
+    m.kp = (float)(nu / (1 - 2 * nu));
+    set_material(s, m);
     return NFX_OK;
 }
 
@@ -384,30 +428,29 @@ int nfx_set_viscoplastic(nfx_sim* s, const double* par) {
     CUDA_TRY(cudaMemsetAsync(s->st.vp_b, 0, ntp * sizeof(float4), s->stream));
     CUDA_TRY(cudaMemsetAsync(s->st.vp_c, 0, ntp * sizeof(float2), s->stream));
     CUDA_TRY(cudaMemsetAsync(s->st.fields, 0, ntp * sizeof(float2), s->stream));
-    s->mat = MaterialDev{};
-    s->mat.model = MODEL_VP;
-    s->mat.mu1 = (float)par[0];
-    s->mat.mu2 = (float)par[1];
-    s->mat.kappa = (float)par[2];
-    s->mat.flow_exp = (float)par[3];
-    s->mat.yield = (float)par[4];
-    s->mat.flow_rate = (float)par[5];
-    s->mat.hard_thr = (float)par[6];
-    s->mat.hard_exp = (float)par[7];
-    s->have_material = true;
-    invalidate_graph(s);
+    MaterialDev m{};
+    m.model = MODEL_VP;
+    m.mu1 = (float)par[0];
+    m.mu2 = (float)par[1];
+    m.kappa = (float)par[2];
+    m.flow_exp = (float)par[3];
+    m.yield = (float)par[4];
+    m.flow_rate = (float)par[5];
+    m.hard_thr = (float)par[6];
+    m.hard_exp = (float)par[7];
+    set_material(s, m);
     return NFX_OK;
 }
 
 int nfx_add_contact(nfx_sim* s, int kind, double k, double radius, double p0, double v, double tmove, int* id) {
     CHECK_ARG(s, "null handle");
     CHECK_ARG(kind == NFX_CONTACT_SUBSTRATE || kind == NFX_CONTACT_PLANE || kind == NFX_CONTACT_SPHERE, "unknown contact kind");
-    CHECK_ARG(s->prm.n_contacts < MAX_CONTACTS, "at most 4 contacts");
+    CHECK_ARG(s->cell.n_contacts < MAX_CONTACTS, "at most 4 contacts");
     CHECK_ARG(std::isfinite(k) && std::isfinite(p0) && std::isfinite(v) && !std::isnan(tmove), "non-finite contact parameter");
     CHECK_ARG(kind != NFX_CONTACT_SPHERE || radius > 0, "sphere radius must be positive");
     int rc;
     if ((rc = set_device(s)) != NFX_OK) return rc;
-    const int i = s->prm.n_contacts;
+    const int i = s->cell.n_contacts;
     if (!s->d_meta[i] && (rc = dalloc(s, &s->d_meta[i], 2, nullptr)) != NFX_OK) return rc;
     CUDA_TRY(cudaMemsetAsync(s->d_meta[i], 0, 2 * sizeof(long long), s->stream));
     ContactDev c{};
@@ -419,16 +462,16 @@ int nfx_add_contact(nfx_sim* s, int kind, double k, double radius, double p0, do
     c.tmove = tmove;
     c.table = s->d_tables[i];
     c.meta = s->d_meta[i];
-    s->prm.c[i] = c;
-    s->prm.n_contacts++;
+    s->cell.c[i] = c;
+    s->cell.n_contacts++;
+    s->cell_dirty = true;
     if (id) *id = i;
-    invalidate_graph(s);
     return NFX_OK;
 }
 
 int nfx_set_contact_table(nfx_sim* s, int id, int64_t t0, int64_t n, const double* pos) {
     CHECK_ARG(s, "null handle");
-    CHECK_ARG(id >= 0 && id < s->prm.n_contacts, "contact id out of range");
+    CHECK_ARG(id >= 0 && id < s->cell.n_contacts, "contact id out of range");
     CHECK_ARG(n >= 0 && (n == 0 || pos), "bad table");
     for (int64_t k = 0; k < n; k++) CHECK_ARG(std::isfinite(pos[k]), "non-finite table position");
     int rc;
@@ -442,8 +485,9 @@ int nfx_set_contact_table(nfx_sim* s, int id, int64_t t0, int64_t n, const doubl
         const long long cap = std::max<long long>(n, 4096);
         if ((rc = dalloc(s, &s->d_tables[id], (size_t)cap, nullptr)) != NFX_OK) return rc;
         s->table_cap[id] = cap;
-        s->prm.c[id].table = s->d_tables[id];
-        invalidate_graph(s);  // the table pointer is a kernel parameter
+        s->cell.c[id].table = s->d_tables[id];
+        s->cell_dirty = true;
+        if ((rc = upload_cell(s)) != NFX_OK) return rc;
     }
     const long long meta[2] = {(long long)t0, (long long)n};
     if (n > 0) CUDA_TRY(cudaMemcpyAsync(s->d_tables[id], pos, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, s->stream));
@@ -456,22 +500,22 @@ int nfx_set_integrator(nfx_sim* s, double xi, int fix_top_bottom) {
     CHECK_ARG(s, "null handle");
     CHECK_ARG(std::isfinite(xi) && xi > -2.0, "bad damping");
     // v' = (v (1 - xi/2) + (f + fo)/2) / (1 + xi/2);  x' = x + v'(1 - xi/2) + f/2  (VelocityVerlet.cl:12-14)
-    s->prm.vv_a = (float)((1 - 0.5 * xi) / (1 + 0.5 * xi));
-    s->prm.vv_hb = (float)(0.5 / (1 + 0.5 * xi));
-    s->prm.vv_dm = (float)(1 - 0.5 * xi);
-    s->prm.fix_a = s->prm.fix_b = -1;
+    if (fix_top_bottom && !s->have_mesh) return fail(NFX_ERR_STATE, "set the mesh before pinning nodes 3 and 4");
+    s->cell.vv_a = (float)((1 - 0.5 * xi) / (1 + 0.5 * xi));
+    s->cell.vv_hb = (float)(0.5 / (1 + 0.5 * xi));
+    s->cell.vv_dm = (float)(1 - 0.5 * xi);
+    s->cell.fix_a = s->cell.fix_b = -1;
     if (fix_top_bottom) {
-        if (!s->have_mesh) return fail(NFX_ERR_STATE, "set the mesh before pinning nodes 3 and 4");
-        if (s->plan.np > 3) s->prm.fix_a = (int)s->plan.node_int[3];
-        if (s->plan.np > 4) s->prm.fix_b = (int)s->plan.node_int[4];
+        if (s->plan.np > 3) s->cell.fix_a = (int)s->plan.node_int[3];
+        if (s->plan.np > 4) s->cell.fix_b = (int)s->plan.node_int[4];
     }
-    invalidate_graph(s);
+    s->cell_dirty = true;
     return NFX_OK;
 }
 
 int nfx_set_record(nfx_sim* s, int contact, int64_t every, int64_t max_rows) {
     CHECK_ARG(s, "null handle");
-    CHECK_ARG(contact >= -1 && contact < s->prm.n_contacts, "contact id out of range");
+    CHECK_ARG(contact >= -1 && contact < s->cell.n_contacts, "contact id out of range");
     CHECK_ARG(contact < 0 || (every > 0 && max_rows > 0), "every and max_rows must be positive");
     int rc;
     if ((rc = set_device(s)) != NFX_OK) return rc;
@@ -484,13 +528,13 @@ int nfx_set_record(nfx_sim* s, int contact, int64_t every, int64_t max_rows) {
         s->curve_rows = max_rows;
     }
     if (s->d_curve) CUDA_TRY(cudaMemsetAsync(s->d_curve, 0, 3 * (size_t)s->curve_rows * sizeof(double), s->stream));
-    s->st.curve = s->d_curve;
-    s->prm.record_contact = contact;
-    s->prm.record_every = contact >= 0 ? every : 0;
-    s->prm.max_rows = contact >= 0 ? max_rows : 0;
-    s->prm.fields_every = every > 0 ? every : 0;
+    s->cell.record_contact = contact;
+    s->cell_dirty = true;
+    s->record_every = contact >= 0 ? every : 0;
+    s->max_rows = contact >= 0 ? max_rows : 0;
+    s->fields_every = every > 0 ? every : 0;
     s->rows_written = 0;
-    invalidate_graph(s);
+    invalidate_graph(s);  // record settings and the curve buffer are kernel arguments
     return NFX_OK;
 }
 
@@ -499,6 +543,7 @@ int nfx_step(nfx_sim* s, int64_t nsteps) {
     if ((rc = require_ready(s)) != NFX_OK) return rc;
     CHECK_ARG(nsteps >= 0, "negative step count");
     if ((rc = set_device(s)) != NFX_OK) return rc;
+    if ((rc = upload_cell(s)) != NFX_OK) return rc;
     const long long t_begin = s->time;
     int64_t left = nsteps;
     while (left >= GRAPH_STEPS) {
@@ -516,8 +561,9 @@ int nfx_record_now(nfx_sim* s) {
     int rc;
     if ((rc = require_ready(s)) != NFX_OK) return rc;
     if ((rc = set_device(s)) != NFX_OK) return rc;
-    if (s->prm.record_contact < 0) return NFX_OK;
-    CUDA_TRY(launch_node_pass(s->mesh, s->st, s->prm, 0, NODE_READOUT_ROW, -1, s->stream));
+    if (s->cell.record_contact < 0) return NFX_OK;
+    if ((rc = upload_cell(s)) != NFX_OK) return rc;
+    CUDA_TRY(launch_nodes(s, 0, NODE_READOUT_ROW, -1));
     note_rows(s, s->time, s->time);
     return NFX_OK;
 }
@@ -590,7 +636,7 @@ int nfx_get_tet_field(nfx_sim* s, int which, double* out) {
     CHECK_ARG(which >= 0 && which <= 2, "unknown field");
     if (!s->have_mesh) return fail(NFX_ERR_STATE, "no mesh");
     const int64_t nt = s->plan.nt, ns = s->plan.nslots;
-    if (s->mat.model != MODEL_VP || !s->st.vp_c) {
+    if (s->cell.mat.model != MODEL_VP || !s->st.vp_c) {
         // the elastic kernel (tetra.cl) writes no per-tetra fields; the reference's buffers stay 0
         std::fill(out, out + nt, 0.0);
         return NFX_OK;
@@ -611,7 +657,7 @@ int nfx_get_plastic_tensor(nfx_sim* s, double* out) {
     CHECK_ARG(s && out, "null argument");
     if (!s->have_mesh) return fail(NFX_ERR_STATE, "no mesh");
     const int64_t nt = s->plan.nt;
-    if (s->mat.model != MODEL_VP || !s->st.vp_a) {
+    if (s->cell.mat.model != MODEL_VP || !s->st.vp_a) {
         for (int k = 0; k < 9; k++)
             for (int64_t t = 0; t < nt; t++) out[k * nt + t] = (k % 4 == 0) ? 1.0 : 0.0;
         return NFX_OK;
@@ -652,9 +698,10 @@ int nfx_indenter_force(nfx_sim* s, int contact, double* out) {
     int rc;
     if ((rc = require_ready(s)) != NFX_OK) return rc;
     CHECK_ARG(out, "null out");
-    CHECK_ARG(contact >= 0 && contact < s->prm.n_contacts, "contact id out of range");
+    CHECK_ARG(contact >= 0 && contact < s->cell.n_contacts, "contact id out of range");
     if ((rc = set_device(s)) != NFX_OK) return rc;
-    CUDA_TRY(launch_node_pass(s->mesh, s->st, s->prm, 0, NODE_READOUT_VALUE, contact, s->stream));
+    if ((rc = upload_cell(s)) != NFX_OK) return rc;
+    CUDA_TRY(launch_nodes(s, 0, NODE_READOUT_VALUE, contact));
     CUDA_TRY(cudaMemcpyAsync(out, s->d_force_out, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     return NFX_OK;
@@ -700,6 +747,7 @@ int nfx_profile_steps(nfx_sim* s, int64_t nsteps, float* tet_ms, float* node_ms)
     int rc;
     if ((rc = require_ready(s)) != NFX_OK) return rc;
     if ((rc = set_device(s)) != NFX_OK) return rc;
+    if ((rc = upload_cell(s)) != NFX_OK) return rc;
     std::vector<cudaEvent_t> ev(3 * (size_t)nsteps + 1);
     for (auto& e : ev) CUDA_TRY(cudaEventCreate(&e));
     const long long t_begin = s->time;
@@ -708,7 +756,7 @@ int nfx_profile_steps(nfx_sim* s, int64_t nsteps, float* tet_ms, float* node_ms)
         cudaEventRecord(ev[3 * k], s->stream);
         err = launch_elem(s, (int)k);
         cudaEventRecord(ev[3 * k + 1], s->stream);
-        if (err == cudaSuccess) err = launch_node_pass(s->mesh, s->st, s->prm, (int)k, NODE_UPDATE, -1, s->stream);
+        if (err == cudaSuccess) err = launch_nodes(s, (int)k, NODE_UPDATE, -1);
         cudaEventRecord(ev[3 * k + 2], s->stream);
     }
     if (err == cudaSuccess) err = launch_advance_time(s->st, nsteps, s->stream);

@@ -210,7 +210,7 @@ int build_device(nfx_batch* b, const std::vector<int>& which, int tile_tets, Bat
 
     auto& A = D.allocs;
     int* d_ttb; int* d_tnb; unsigned* d_tm; uint2* d_tn; uchar4* d_lc; ushort4* d_ti; float4 *d_da, *d_db; float2* d_dc;
-    float4 *d_xh, *d_xl, *d_uh, *d_ul, *d_v, *d_fo; unsigned long long* d_fa; double* d_part;
+    float4 *d_xh, *d_xl, *d_uh, *d_ul, *d_v, *d_fo; unsigned long long* d_fa; double* d_part; double* d_fout;
     CellDev* d_cells; int *d_tc, *d_bc; unsigned* d_cc; double* d_curves = nullptr;
     float4 *d_pa = nullptr, *d_pb = nullptr; float2 *d_pc = nullptr, *d_fields = nullptr;
     int rc;
@@ -220,7 +220,7 @@ int build_device(nfx_batch* b, const std::vector<int>& which, int tile_tets, Bat
         (rc = balloc(A, &d_da, ntp)) || (rc = balloc(A, &d_db, ntp)) || (rc = balloc(A, &d_dc, ntp)) ||
         (rc = balloc(A, &d_xh, np)) || (rc = balloc(A, &d_xl, np)) || (rc = balloc(A, &d_uh, np)) ||
         (rc = balloc(A, &d_ul, np)) || (rc = balloc(A, &d_v, np)) || (rc = balloc(A, &d_fo, np)) ||
-        (rc = balloc(A, &d_fa, 3 * (size_t)np)) || (rc = balloc(A, &d_part, nblocks)) ||
+        (rc = balloc(A, &d_fa, 3 * (size_t)np)) || (rc = balloc(A, &d_part, nblocks)) || (rc = balloc(A, &d_fout, cells.size())) ||
         (rc = balloc(A, &d_cells, cells.size())) || (rc = balloc(A, &d_tc, ntiles)) || (rc = balloc(A, &d_bc, nblocks)) ||
         (rc = balloc(A, &d_cc, cells.size())) || (rc = balloc(A, &d_curves, 3 * rows * cells.size())) ||
         (rc = balloc(A, &D.d_time, 1)) || (rc = balloc(A, &D.d_status, 1)))
@@ -289,6 +289,7 @@ int build_device(nfx_batch* b, const std::vector<int>& which, int tile_tets, Bat
     S.status = D.d_status;
     S.time = D.d_time;
     S.partials = d_part;
+    S.force_out = d_fout;
     BatchDev& B = D.bd;
     B.cells = d_cells;
     B.tile_cell = d_tc;
@@ -304,8 +305,8 @@ int build_device(nfx_batch* b, const std::vector<int>& which, int tile_tets, Bat
 
 int enqueue_batch_steps(nfx_batch* b, BatchDevice& D, int n) {
     for (int k = 0; k < n; k++) {
-        BCUDA(launch_tet_pass_batch(D.mesh, D.st, D.bd, b->model, k, b->stream));
-        BCUDA(launch_node_pass_batch(D.mesh, D.st, D.bd, D.nblocks, k, NODE_UPDATE, b->stream));
+        BCUDA(launch_tet_pass(D.mesh, D.st, D.bd, b->model, k, b->stream));
+        BCUDA(launch_node_pass(D.mesh, D.st, D.bd, D.nblocks, k, NODE_UPDATE, -1, b->stream));
     }
     BCUDA(launch_advance_time(D.st, n, b->stream));
     return NFX_OK;
@@ -623,8 +624,19 @@ int nfx_batch_record_now(nfx_batch* b) {
     BARG(b, "null batch");
     if (!b->finalized) return bfail(NFX_ERR_STATE, "call nfx_batch_finalize first");
     BCUDA(cudaSetDevice(b->device));
-    BCUDA(launch_node_pass_batch(b->dev.mesh, b->dev.st, b->dev.bd, b->dev.nblocks, 0, NODE_READOUT_ROW, b->stream));
+    BCUDA(launch_node_pass(b->dev.mesh, b->dev.st, b->dev.bd, b->dev.nblocks, 0, NODE_READOUT_ROW, -1, b->stream));
     note_batch_rows(b, b->time, b->time);
+    return NFX_OK;
+}
+
+int nfx_batch_indenter_force(nfx_batch* b, int contact, double* out) {
+    BARG(b && out, "null argument");
+    BARG(contact >= 0 && contact < MAX_CONTACTS, "contact id out of range");
+    if (!b->finalized) return bfail(NFX_ERR_STATE, "call nfx_batch_finalize first");
+    BCUDA(cudaSetDevice(b->device));
+    BCUDA(launch_node_pass(b->dev.mesh, b->dev.st, b->dev.bd, b->dev.nblocks, 0, NODE_READOUT_VALUE, contact, b->stream));
+    BCUDA(cudaMemcpyAsync(out, b->dev.st.force_out, b->cells.size() * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+    BCUDA(cudaStreamSynchronize(b->stream));
     return NFX_OK;
 }
 

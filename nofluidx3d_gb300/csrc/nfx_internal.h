@@ -102,10 +102,8 @@ struct StateDev {
     float2* fields; // von Mises, pressure per tetra (viscoplastic model)
     unsigned* status;
     long long* time;     // simulation time at the start of the current graph chunk
-    double* curve;       // 3 * max_rows: (t, indentation, force)
     double* partials;    // one per node block, for the deterministic readout reduction
-    unsigned* counter;   // blocks finished in the readout reduction
-    double* force_out;   // scalar result of an on-demand readout
+    double* force_out;   // per cell: result of an on-demand readout
 };
 
 struct ContactDev {
@@ -127,20 +125,12 @@ struct MaterialDev {
     float flow_exp, yield, flow_rate, hard_thr, hard_exp;
 };
 
-struct StepParams {
-    int n_contacts;
-    ContactDev c[MAX_CONTACTS];
-    int record_contact;        // -1: no force recording
-    long long record_every;    // 0: none
-    long long max_rows;
-    long long fields_every;    // tet fields written when (t+1) % fields_every == 0
-    float vv_a, vv_hb, vv_dm;  // v' = a v + hb (f + fo); dx = dm v' + f/2
-    int fix_a, fix_b;          // internal ids of the pinned nodes, -1 if none
-};
-
 // ---------------------------------------------------------------------------------------
-// Batched cells: one set of concatenated tile/tetra/node arrays for many independent cells,
-// with per-cell parameters looked up per tile (element pass) and per node block (node pass).
+// Per-cell parameters. The kernels read every material, contact and integrator parameter from
+// a device table of cells, never from kernel arguments: a single simulation is a table of one
+// cell, a batch concatenates many cells' tile/tetra/node arrays and maps each tile and each node
+// block to its cell. Both therefore run the same kernels with the same arithmetic, and a
+// captured CUDA graph stays valid when the host rewrites a parameter in the table.
 // Each cell's nodes occupy whole node blocks, so a node block belongs to exactly one cell.
 // ---------------------------------------------------------------------------------------
 struct CellDev {
@@ -156,34 +146,32 @@ struct CellDev {
 
 struct BatchDev {
     const CellDev* cells;
-    const int* tile_cell;        // per tile
-    const int* block_cell;       // per node block
+    const int* tile_cell;        // per tile; null: every tile belongs to cell 0
+    const int* block_cell;       // per node block; null: every block belongs to cell 0
     unsigned* cell_counter;      // per cell: blocks finished in the readout reduction
     double* curves;              // per cell: max_rows rows of (t, indentation, force)
-    long long record_every, max_rows, fields_every;
+    long long record_every;      // 0: no force recording
+    long long max_rows;
+    long long fields_every;      // tet fields written when (t+1) % fields_every == 0
 };
 
 // Sets the message nfx_last_error() returns on this thread (nfx_api.cpp).
 void set_error(const std::string& msg);
 
-// Batched launches (nfx_kernels.cu): element pass over all tiles of all cells, node pass over
-// all node blocks.
-cudaError_t launch_tet_pass_batch(const MeshDev& m, const StateDev& s, const BatchDev& b, int model, int t_offset,
-                                  cudaStream_t stream);
-cudaError_t launch_node_pass_batch(const MeshDev& m, const StateDev& s, const BatchDev& b, int nblocks, int t_offset,
-                                   int mode, cudaStream_t stream);
-
 // Kernel launchers (nfx_kernels.cu). All enqueue on `stream` and return cudaGetLastError().
-cudaError_t launch_tet_pass(const MeshDev& m, const StateDev& s, const MaterialDev& mat, const StepParams& p,
-                            int t_offset, cudaStream_t stream);
-// Persistent, bulk-copy-pipelined element pass: `grid` CTAs walk all tiles.
-cudaError_t launch_tet_pass_pipe(const MeshDev& m, const StateDev& s, const MaterialDev& mat, const StepParams& p,
-                                 int t_offset, int grid, cudaStream_t stream);
+// Element pass over all tiles (one CTA per tile), material from the cell table.
+cudaError_t launch_tet_pass(const MeshDev& m, const StateDev& s, const BatchDev& b, int model, int t_offset,
+                            cudaStream_t stream);
+// Persistent, bulk-copy-pipelined element pass of a one-cell table: `grid` CTAs walk all tiles.
+cudaError_t launch_tet_pass_pipe(const MeshDev& m, const StateDev& s, const BatchDev& b, int model, int t_offset,
+                                 int grid, cudaStream_t stream);
 // Resident CTAs per SM of the pipelined element pass for a material model and tile size.
 int pipe_blocks_per_sm(int model, int tile);
 enum NodeMode : int { NODE_UPDATE = 0, NODE_READOUT_ROW = 1, NODE_READOUT_VALUE = 2 };
-cudaError_t launch_node_pass(const MeshDev& m, const StateDev& s, const StepParams& p, int t_offset, int mode,
-                             int readout_contact, cudaStream_t stream);
+// Node pass over `nblocks` node blocks. NODE_READOUT_VALUE sums contact `readout_contact`'s force
+// per cell into force_out[cell] without updating the state.
+cudaError_t launch_node_pass(const MeshDev& m, const StateDev& s, const BatchDev& b, int nblocks, int t_offset,
+                             int mode, int readout_contact, cudaStream_t stream);
 cudaError_t launch_advance_time(const StateDev& s, long long n, cudaStream_t stream);
 // Conversions between the user's layout (SoA doubles, user order) and the device state.
 cudaError_t launch_points_to_user(const MeshDev& m, const StateDev& s, const long long* node_user, double* out,

@@ -126,11 +126,11 @@ __device__ __forceinline__ bool fields_due(const StateDev& s, long long fields_e
 // ------------------------------------------------------------------------------------------
 // Element pass, one CTA per tile (plain loads)
 // ------------------------------------------------------------------------------------------
-// BATCHED: tiles of many cells in one launch; each tile takes its cell's material from the
-// batch's parameter table instead of `mat`.
-template <int MODEL, int TILE, bool BATCHED>
+// The tile's material comes from its cell's entry in the cell table (cell 0 when the table has
+// no tile map), so a single simulation and a batch run this same code.
+template <int MODEL, int TILE>
 __global__ void __launch_bounds__(TILE, 65536 / (TILE * 64))
-    k_tet_pass(MeshDev m, StateDev s, MaterialDev mat, BatchDev bd, long long fields_every, int t_offset) {
+    k_tet_pass(MeshDev m, StateDev s, BatchDev bd, int t_offset) {
     constexpr int NMAX = TILE < TILE_NODES_MAX ? TILE : TILE_NODES_MAX;
     __shared__ float4 s_uh[NMAX];
     __shared__ float4 s_ul[NMAX];
@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * 64))
     const int ntt = (int)(meta & 0xffffu);
     const int nn = (int)(meta >> 16);
     const bool act = j < ntt;
-    const bool wf = fields_due(s, fields_every, t_offset);
+    const bool wf = fields_due(s, bd.fields_every, t_offset);
 
     // Streaming per-tetra data (read once per step: evict-first) and the node list, issued for
     // every slot and entry without waiting for the meta word: padding is valid zeroed memory.
@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * 64))
         s_uh[j] = s.uh[node.x];
         s_ul[j] = s.ul[node.x];
     }
-    if (BATCHED) mat = bd.cells[bd.tile_cell[b]].mat;
+    const MaterialDev mat = bd.cells[bd.tile_cell ? __ldg(bd.tile_cell + b) : 0].mat;
     __syncthreads();
     if (act) element_eval<MODEL>(j, t, lc, da, db, dc, pa, pb, pc, s_uh, s_ul, s_cf, s, mat, wf);
     __syncthreads();
@@ -269,9 +269,12 @@ template <int MODEL, int TILE>
 __device__ __forceinline__ void issue_tile(const MeshDev& m, const StateDev& s, int tile, unsigned char* st,
                                            StageHdr* hdr, unsigned long long* bar) {
     using StageLayout = nfx::StageLayout<TILE>;
-    const int tb = m.tile_tet_begin[tile], ntt = m.tile_tet_begin[tile + 1] - tb;
-    const int nb = m.tile_node_begin[tile], nn = m.tile_node_begin[tile + 1] - nb;
-    const int nb0 = nb & ~1;          // 16-byte aligned start of the node list
+    // fixed-stride tiles: slots from tile*TILE, node entries from tile*NMAX (NMAX even, so the
+    // node list starts on a 16-byte boundary); real counts from the meta word
+    const unsigned meta = m.tile_meta[tile];
+    const int tb = tile * TILE, ntt = (int)(meta & 0xffffu);
+    const int nb = tile * StageLayout::NMAX, nn = (int)(meta >> 16);
+    const int nb0 = nb & ~1;
     const int noff = nb - nb0;
     const unsigned nodes_b = round16(8u * (unsigned)(nn + noff));
     const unsigned b4 = round16(4u * ntt), b8 = round16(8u * ntt), b16 = 16u * ntt;
@@ -311,8 +314,7 @@ __device__ __forceinline__ void gather_nodes(const StateDev& s, unsigned char* s
 }
 
 template <int MODEL, int TILE>
-__global__ void __launch_bounds__(TILE) k_tet_pass_pipe(MeshDev m, StateDev s, MaterialDev mat,
-                                                        long long fields_every, int t_offset) {
+__global__ void __launch_bounds__(TILE) k_tet_pass_pipe(MeshDev m, StateDev s, BatchDev bd, int t_offset) {
     using StageLayout = nfx::StageLayout<TILE>;
     extern __shared__ __align__(128) unsigned char smem[];
     constexpr unsigned SB = pipe_stage_bytes<TILE>(MODEL);
@@ -326,7 +328,8 @@ __global__ void __launch_bounds__(TILE) k_tet_pass_pipe(MeshDev m, StateDev s, M
     const int j = threadIdx.x;
     const int G = gridDim.x;
     const int first = blockIdx.x;
-    const bool wf = fields_due(s, fields_every, t_offset);
+    const bool wf = fields_due(s, bd.fields_every, t_offset);
+    const MaterialDev mat = bd.cells[0].mat;
     if (first >= m.ntiles) return;
 
     if (j == 0) {
@@ -408,49 +411,6 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
-}
-
-// Fixed-order grid reduction of one double per thread. The last block to finish sums the
-// per-block partials in index order, so the result is the same on every run.
-__device__ void grid_sum_finish(const StateDev& s, double val, bool to_scalar, long long row, long long t,
-                                double indentation) {
-    __shared__ double s_w[NODE_BLOCK / 32];
-    __shared__ int s_last;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    val = warp_sum_d(val);
-    if (lane == 0) s_w[warp] = val;
-    __syncthreads();
-    if (warp == 0) {
-        double x = lane < NODE_BLOCK / 32 ? s_w[lane] : 0.0;
-        x = warp_sum_d(x);
-        if (lane == 0) {
-            s.partials[blockIdx.x] = x;
-            __threadfence();
-            const unsigned prev = atomicAdd(s.counter, 1u);
-            s_last = prev == gridDim.x - 1;
-        }
-    }
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
-    double acc = 0.0;
-    const volatile double* part = s.partials;
-    for (int k = threadIdx.x; k < (int)gridDim.x; k += NODE_BLOCK) acc += part[k];
-    acc = warp_sum_d(acc);
-    if (lane == 0) s_w[warp] = acc;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double tot = 0.0;
-        for (int w = 0; w < NODE_BLOCK / 32; w++) tot += s_w[w];
-        if (to_scalar) {
-            *s.force_out = tot;
-        } else {
-            s.curve[3 * row] = (double)t;
-            s.curve[3 * row + 1] = indentation;
-            s.curve[3 * row + 2] = tot;
-        }
-        *s.counter = 0u;
-    }
 }
 
 // Contact force on one node in double precision (the reference's FP64 formulas). Returns the
@@ -543,8 +503,20 @@ __device__ __forceinline__ double node_step(const MeshDev& m, const StateDev& s,
     return ro;
 }
 
-__global__ void __launch_bounds__(NODE_BLOCK) k_node_pass(MeshDev m, StateDev s, StepParams p, int t_offset,
-                                                          int mode, int readout_contact) {
+// One thread per node. The block's cell (cell 0 without a block map) supplies the contacts and
+// the integrator. On record steps (and for on-demand readouts) the readout values are summed per
+// cell in a fixed order: warp shuffles, then the block's warps in order, then — by the cell's
+// last block to finish — the cell's block partials in index order, so the result is the same on
+// every run and does not depend on which other cells share the launch.
+#ifndef NFX_NODE_MIN_BLOCKS
+#define NFX_NODE_MIN_BLOCKS 1  // resident node-pass blocks per SM the register allocation must allow
+#endif
+__global__ void __launch_bounds__(NODE_BLOCK, NFX_NODE_MIN_BLOCKS) k_node_pass(MeshDev m, StateDev s, BatchDev bd, int t_offset, int mode,
+                                                          int readout_contact) {
+    __shared__ double s_w[NODE_BLOCK / 32];
+    __shared__ int s_last;
+    const int cell = bd.block_cell ? __ldg(bd.block_cell + blockIdx.x) : 0;
+    const CellDev& C = bd.cells[cell];
     const int i = blockIdx.x * NODE_BLOCK + threadIdx.x;
     const long long t = *s.time + t_offset;
     int rc;
@@ -554,45 +526,14 @@ __global__ void __launch_bounds__(NODE_BLOCK) k_node_pass(MeshDev m, StateDev s,
         rc = readout_contact;
         rec = true;
     } else {
-        rc = p.record_contact;
-        rec = rc >= 0 && p.record_every > 0 && (t % p.record_every) == 0;
+        rc = C.record_contact;
+        rec = rc >= 0 && bd.record_every > 0 && (t % bd.record_every) == 0;
         if (rec) {
-            row = t / p.record_every;
-            if (row >= p.max_rows) {
-                if (i == 0) atomicOr(s.status, STATUS_CURVE_FULL);
+            row = t / bd.record_every;
+            if (row >= bd.max_rows) {
+                if (threadIdx.x == 0) atomicOr(s.status, STATUS_CURVE_FULL);
                 rec = false;
             }
-        }
-    }
-    double ro = 0.0;
-    if (i < m.np)
-        ro = node_step(m, s, i, t, p.c, p.n_contacts, rc, p.vv_a, p.vv_hb, p.vv_dm, p.fix_a, p.fix_b,
-                       mode == NODE_UPDATE);
-    if (rec) {
-        double ind = 0.0;
-        if (rc >= 0 && rc < p.n_contacts) ind = contact_pos(p.c[rc], 0) - contact_pos(p.c[rc], t);
-        grid_sum_finish(s, ro, mode == NODE_READOUT_VALUE, row, t, ind);
-    }
-}
-
-// Batched node pass: block -> cell, the cell's parameters from the batch table, and a per-cell
-// fixed-order readout (the cell's last block to finish sums the cell's block partials in order).
-__global__ void __launch_bounds__(NODE_BLOCK) k_node_pass_batch(MeshDev m, StateDev s, BatchDev bd, int t_offset,
-                                                                int mode) {
-    __shared__ double s_w[NODE_BLOCK / 32];
-    __shared__ int s_last;
-    const int cell = bd.block_cell[blockIdx.x];
-    const CellDev& C = bd.cells[cell];
-    const int i = blockIdx.x * NODE_BLOCK + threadIdx.x;
-    const long long t = *s.time + t_offset;
-    const int rc = C.record_contact;
-    bool rec = rc >= 0 && bd.record_every > 0 && (t % bd.record_every) == 0;
-    long long row = 0;
-    if (rec) {
-        row = t / bd.record_every;
-        if (row >= bd.max_rows) {
-            if (threadIdx.x == 0) atomicOr(s.status, STATUS_CURVE_FULL);
-            rec = false;
         }
     }
     double ro = 0.0;
@@ -626,10 +567,14 @@ __global__ void __launch_bounds__(NODE_BLOCK) k_node_pass_batch(MeshDev m, State
     if (threadIdx.x == 0) {
         double tot = 0.0;
         for (int w = 0; w < NODE_BLOCK / 32; w++) tot += s_w[w];
-        double* r = bd.curves + 3 * ((long long)cell * bd.max_rows + row);
-        r[0] = (double)t;
-        r[1] = contact_pos(C.c[rc], 0) - contact_pos(C.c[rc], t);
-        r[2] = tot;
+        if (mode == NODE_READOUT_VALUE) {
+            s.force_out[cell] = tot;
+        } else {
+            double* r = bd.curves + 3 * ((long long)cell * bd.max_rows + row);
+            r[0] = (double)t;
+            r[1] = contact_pos(C.c[rc], 0) - contact_pos(C.c[rc], t);
+            r[2] = tot;
+        }
         bd.cell_counter[cell] = 0u;
     }
 }
@@ -683,8 +628,8 @@ __global__ void k_vec_from_user(int np, float4* a, const long long* node_user, c
 // Launchers
 // ------------------------------------------------------------------------------------------
 template <int MODEL, int TILE>
-static cudaError_t launch_pipe(const MeshDev& m, const StateDev& s, const MaterialDev& mat, const StepParams& p,
-                               int t_offset, int grid, cudaStream_t st) {
+static cudaError_t launch_pipe(const MeshDev& m, const StateDev& s, const BatchDev& b, int t_offset, int grid,
+                               cudaStream_t st) {
     const unsigned bytes = pipe_smem_bytes<TILE>(MODEL);
     static bool attr_set = false;  // per process; the attribute is per function
     if (!attr_set) {
@@ -693,7 +638,7 @@ static cudaError_t launch_pipe(const MeshDev& m, const StateDev& s, const Materi
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
-    k_tet_pass_pipe<MODEL, TILE><<<grid, TILE, bytes, st>>>(m, s, mat, p.fields_every, t_offset);
+    k_tet_pass_pipe<MODEL, TILE><<<grid, TILE, bytes, st>>>(m, s, b, t_offset);
     return cudaGetLastError();
 }
 
@@ -724,88 +669,56 @@ int pipe_blocks_per_sm(int model, int tile) {
 }
 
 template <int TILE>
-static cudaError_t launch_pipe_tile(const MeshDev& m, const StateDev& s, const MaterialDev& mat, const StepParams& p,
-                                    int t_offset, int grid, cudaStream_t st) {
-    switch (mat.model) {
-        case MODEL_MR: return launch_pipe<MODEL_MR, TILE>(m, s, mat, p, t_offset, grid, st);
-        case MODEL_SVK: return launch_pipe<MODEL_SVK, TILE>(m, s, mat, p, t_offset, grid, st);
-        case MODEL_SVKK: return launch_pipe<MODEL_SVKK, TILE>(m, s, mat, p, t_offset, grid, st);
-        case MODEL_VP: return launch_pipe<MODEL_VP, TILE>(m, s, mat, p, t_offset, grid, st);
-        default: return cudaErrorInvalidValue;
-    }
-}
-
-cudaError_t launch_tet_pass_pipe(const MeshDev& m, const StateDev& s, const MaterialDev& mat, const StepParams& p,
-                                 int t_offset, int grid, cudaStream_t st) {
-    switch (m.tile_tets) {
-        case 64: return launch_pipe_tile<64>(m, s, mat, p, t_offset, grid, st);
-        case 128: return launch_pipe_tile<128>(m, s, mat, p, t_offset, grid, st);
-        case 256: return launch_pipe_tile<256>(m, s, mat, p, t_offset, grid, st);
-        default: return cudaErrorInvalidValue;
-    }
-}
-
-template <int TILE>
-static cudaError_t launch_tile(const MeshDev& m, const StateDev& s, const MaterialDev& mat, const StepParams& p,
-                               int t_offset, cudaStream_t st) {
-    const dim3 grid((unsigned)m.ntiles), block(TILE);
-    switch (mat.model) {
-        case MODEL_MR: k_tet_pass<MODEL_MR, TILE, false><<<grid, block, 0, st>>>(m, s, mat, BatchDev{}, p.fields_every, t_offset); break;
-        case MODEL_SVK: k_tet_pass<MODEL_SVK, TILE, false><<<grid, block, 0, st>>>(m, s, mat, BatchDev{}, p.fields_every, t_offset); break;
-        case MODEL_SVKK: k_tet_pass<MODEL_SVKK, TILE, false><<<grid, block, 0, st>>>(m, s, mat, BatchDev{}, p.fields_every, t_offset); break;
-        case MODEL_VP: k_tet_pass<MODEL_VP, TILE, false><<<grid, block, 0, st>>>(m, s, mat, BatchDev{}, p.fields_every, t_offset); break;
-        default: return cudaErrorInvalidValue;
-    }
-    return cudaGetLastError();
-}
-
-cudaError_t launch_tet_pass(const MeshDev& m, const StateDev& s, const MaterialDev& mat, const StepParams& p,
-                            int t_offset, cudaStream_t st) {
-    switch (m.tile_tets) {
-        case 64: return launch_tile<64>(m, s, mat, p, t_offset, st);
-        case 128: return launch_tile<128>(m, s, mat, p, t_offset, st);
-        case 256: return launch_tile<256>(m, s, mat, p, t_offset, st);
-        case 512: return launch_tile<512>(m, s, mat, p, t_offset, st);
-        default: return cudaErrorInvalidValue;
-    }
-}
-
-template <int TILE>
-static cudaError_t launch_tile_batch(const MeshDev& m, const StateDev& s, const BatchDev& b, int model, int t_offset,
-                                     cudaStream_t st) {
-    const dim3 grid((unsigned)m.ntiles), block(TILE);
-    const MaterialDev mat{};
+static cudaError_t launch_pipe_tile(const MeshDev& m, const StateDev& s, const BatchDev& b, int model, int t_offset,
+                                    int grid, cudaStream_t st) {
     switch (model) {
-        case MODEL_MR: k_tet_pass<MODEL_MR, TILE, true><<<grid, block, 0, st>>>(m, s, mat, b, b.fields_every, t_offset); break;
-        case MODEL_SVK: k_tet_pass<MODEL_SVK, TILE, true><<<grid, block, 0, st>>>(m, s, mat, b, b.fields_every, t_offset); break;
-        case MODEL_SVKK: k_tet_pass<MODEL_SVKK, TILE, true><<<grid, block, 0, st>>>(m, s, mat, b, b.fields_every, t_offset); break;
-        case MODEL_VP: k_tet_pass<MODEL_VP, TILE, true><<<grid, block, 0, st>>>(m, s, mat, b, b.fields_every, t_offset); break;
+        case MODEL_MR: return launch_pipe<MODEL_MR, TILE>(m, s, b, t_offset, grid, st);
+        case MODEL_SVK: return launch_pipe<MODEL_SVK, TILE>(m, s, b, t_offset, grid, st);
+        case MODEL_SVKK: return launch_pipe<MODEL_SVKK, TILE>(m, s, b, t_offset, grid, st);
+        case MODEL_VP: return launch_pipe<MODEL_VP, TILE>(m, s, b, t_offset, grid, st);
         default: return cudaErrorInvalidValue;
     }
-    return cudaGetLastError();
 }
 
-cudaError_t launch_tet_pass_batch(const MeshDev& m, const StateDev& s, const BatchDev& b, int model, int t_offset,
-                                  cudaStream_t st) {
+cudaError_t launch_tet_pass_pipe(const MeshDev& m, const StateDev& s, const BatchDev& b, int model, int t_offset,
+                                 int grid, cudaStream_t st) {
     switch (m.tile_tets) {
-        case 64: return launch_tile_batch<64>(m, s, b, model, t_offset, st);
-        case 128: return launch_tile_batch<128>(m, s, b, model, t_offset, st);
-        case 256: return launch_tile_batch<256>(m, s, b, model, t_offset, st);
-        case 512: return launch_tile_batch<512>(m, s, b, model, t_offset, st);
+        case 64: return launch_pipe_tile<64>(m, s, b, model, t_offset, grid, st);
+        case 128: return launch_pipe_tile<128>(m, s, b, model, t_offset, grid, st);
+        case 256: return launch_pipe_tile<256>(m, s, b, model, t_offset, grid, st);
         default: return cudaErrorInvalidValue;
     }
 }
 
-cudaError_t launch_node_pass_batch(const MeshDev& m, const StateDev& s, const BatchDev& b, int nblocks, int t_offset,
-                                   int mode, cudaStream_t st) {
-    k_node_pass_batch<<<nblocks, NODE_BLOCK, 0, st>>>(m, s, b, t_offset, mode);
+template <int TILE>
+static cudaError_t launch_tile(const MeshDev& m, const StateDev& s, const BatchDev& b, int model, int t_offset,
+                               cudaStream_t st) {
+    const dim3 grid((unsigned)m.ntiles), block(TILE);
+    switch (model) {
+        case MODEL_MR: k_tet_pass<MODEL_MR, TILE><<<grid, block, 0, st>>>(m, s, b, t_offset); break;
+        case MODEL_SVK: k_tet_pass<MODEL_SVK, TILE><<<grid, block, 0, st>>>(m, s, b, t_offset); break;
+        case MODEL_SVKK: k_tet_pass<MODEL_SVKK, TILE><<<grid, block, 0, st>>>(m, s, b, t_offset); break;
+        case MODEL_VP: k_tet_pass<MODEL_VP, TILE><<<grid, block, 0, st>>>(m, s, b, t_offset); break;
+        default: return cudaErrorInvalidValue;
+    }
     return cudaGetLastError();
 }
 
-cudaError_t launch_node_pass(const MeshDev& m, const StateDev& s, const StepParams& p, int t_offset, int mode,
-                             int readout_contact, cudaStream_t st) {
-    const unsigned blocks = (unsigned)((m.np + NODE_BLOCK - 1) / NODE_BLOCK);
-    k_node_pass<<<blocks, NODE_BLOCK, 0, st>>>(m, s, p, t_offset, mode, readout_contact);
+cudaError_t launch_tet_pass(const MeshDev& m, const StateDev& s, const BatchDev& b, int model, int t_offset,
+                            cudaStream_t st) {
+    switch (m.tile_tets) {
+        case 64: return launch_tile<64>(m, s, b, model, t_offset, st);
+        case 128: return launch_tile<128>(m, s, b, model, t_offset, st);
+        case 256: return launch_tile<256>(m, s, b, model, t_offset, st);
+        case 512: return launch_tile<512>(m, s, b, model, t_offset, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_node_pass(const MeshDev& m, const StateDev& s, const BatchDev& b, int nblocks, int t_offset,
+                             int mode, int readout_contact, cudaStream_t st) {
+    if (nblocks <= 0) return cudaSuccess;
+    k_node_pass<<<nblocks, NODE_BLOCK, 0, st>>>(m, s, b, t_offset, mode, readout_contact);
     return cudaGetLastError();
 }
 

@@ -46,7 +46,7 @@ class Workload:
     indenter: str = "plane"     # "plane" or "sphere"
     sphere_radius: float = 16.0
     speed: float = 1e-4
-    d0: float = 0.0             # InitialDistance
+    d0: float | None = 0.0      # InitialDistance; None: top node's height - radius (see initial_distance)
     k: float = 0.1              # def_FORCE_CONST
     xi: float = 1e-2            # velocity damping
     steps: int = 20000
@@ -74,15 +74,29 @@ class Workload:
         return (2.0 * self.C10, 2.0 * self.C01, self.K, 1.0, self.yield_stress,
                 self.yield_stress / self.viscosity, 1.0, 0.0)
 
-    def contacts(self) -> list[dict]:
+    def initial_distance(self, mesh: CellMesh | None = None) -> float:
+        """InitialDistance of the walls (Simulation.py:107, :118, :162). With d0 = None it is the
+        top node's height above the radius, so that the substrate (at -(R + d0)) and the indenter
+        (at R + d0, plus the sphere radius) start tangent to the mesh's lowest and highest nodes
+        (nodes 4 and 3, which the Kuhn sphere places symmetrically). A lattice sphere of
+        non-integer radius has its top node up to one spacing above R: walls placed at +-R would
+        start inside the mesh and kick soft cells apart on the first step."""
+        if self.d0 is not None:
+            return float(self.d0)
+        if mesh is None:
+            raise ValueError("d0 = None needs the mesh to place the walls")
+        return float(mesh.points[3, 1]) - self.radius
+
+    def contacts(self, mesh: CellMesh | None = None) -> list[dict]:
         """Substrate first, then the indenter (the recorded contact, index 1)."""
         R = self.radius
-        out = [dict(kind=0, k=self.k, radius=0.0, p0=-(R + self.d0), v=0.0, tmove=float("inf"))]
+        d0 = self.initial_distance(mesh)
+        out = [dict(kind=0, k=self.k, radius=0.0, p0=-(R + d0), v=0.0, tmove=float("inf"))]
         if self.indenter == "plane":
-            out.append(dict(kind=1, k=self.k, radius=0.0, p0=R + self.d0, v=self.speed, tmove=float("inf")))
+            out.append(dict(kind=1, k=self.k, radius=0.0, p0=R + d0, v=self.speed, tmove=float("inf")))
         else:
             Rs = self.sphere_radius
-            out.append(dict(kind=2, k=self.k, radius=Rs, p0=R + Rs + self.d0, v=self.speed, tmove=float("inf")))
+            out.append(dict(kind=2, k=self.k, radius=Rs, p0=R + Rs + d0, v=self.speed, tmove=float("inf")))
         return out
 
     @property
@@ -98,7 +112,7 @@ class Workload:
         else:
             model, E, nu, mr = self.tetra_params()
             sim.set_tetra(model, E, nu, mr)
-        for c in self.contacts():
+        for c in self.contacts(m):
             sim.add_contact(c["kind"], c["k"], c["radius"], c["p0"], c["v"], c["tmove"])
         sim.set_integrator(self.xi, False)
         rows = max_rows if max_rows is not None else self.steps // self.record_every + 1
@@ -114,7 +128,7 @@ class Workload:
         else:
             model, E, nu, mr = self.tetra_params()
             batch.set_tetra(cell, model, E, nu, mr)
-        for c in self.contacts():
+        for c in self.contacts(m):
             batch.add_contact(cell, c["kind"], c["k"], c["radius"], c["p0"], c["v"], c["tmove"])
         batch.set_integrator(cell, self.xi, False)
         return cell
@@ -157,7 +171,8 @@ def batched_cells(n: int = 256, seed: int = 0, r_range=(6.0, 40.0), steps: int =
     (seed + cell index), and per-cell material drawn log-uniform — shear modulus 2e-4..5e-3,
     bulk/shear ratio 5..50, yield stress 5e-5..1e-3, plastic viscosity 1e-2..1e-1 — with the
     viscoplastic law (elastic part Neo-Hookean: mu1 = shear modulus, mu2 = 0). Each cell rests
-    on a substrate and is indented by a sphere of a quarter of its radius at 1e-4 per step."""
+    on a substrate and is indented by a sphere of a quarter of its radius at 1e-4 per step; the
+    walls start tangent to the cell's top and bottom nodes (d0 = None)."""
     import numpy as np
 
     rng = np.random.default_rng(seed)
@@ -174,5 +189,6 @@ def batched_cells(n: int = 256, seed: int = 0, r_range=(6.0, 40.0), steps: int =
     for i in range(n):
         out.append(Workload(f"batched cell {i}", radius=float(R[i]), material="mr_vp", C10=float(mu[i]) / 2.0,
                             C01=0.0, K=float(mu[i] * ratio[i]), yield_stress=float(Y[i]), viscosity=float(eta[i]),
-                            indenter="sphere", sphere_radius=float(R[i]) / 4.0, steps=steps, seed=seed + i))
+                            indenter="sphere", sphere_radius=float(R[i]) / 4.0, steps=steps, seed=seed + i,
+                            d0=None))
     return out

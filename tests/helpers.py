@@ -11,7 +11,7 @@ from nofluidx3d_gb300.workloads import Workload
 def oracle_problem(w: Workload, mesh=None) -> O.Problem:
     m = mesh if mesh is not None else w.mesh()
     contacts = [O.Contact(c["kind"], c["k"], p0=c["p0"], v=c["v"], tmove=min(c["tmove"], 1e300), radius=c["radius"])
-                for c in w.contacts()]
+                for c in w.contacts(m)]
     if w.material == "mr_vp":
         return O.Problem(m.points, m.tets, model=O.MODEL_VP, vp_par=w.vp_params(), contacts=contacts, xi=w.xi,
                          record_contact=w.record_contact)

@@ -14,12 +14,13 @@ pytestmark = pytest.mark.gpu
 
 def small_population():
     cells = batched_cells(4, seed=7, r_range=(2.5, 4.0), steps=250)
-    # faster indentation so short runs produce forces; one elastic-only look-alike is not mixed in
+    # faster indentation so short runs produce forces
     return [w.with_(speed=1e-3, record_every=50) for w in cells]
 
 
 def test_batch_equals_cells_run_alone_bitwise(monkeypatch):
-    """Same tile size as the plain path's default (128): same plans, same arithmetic."""
+    """Same tile size as the plain path's default (128): same plans, and the same kernels (the
+    plain path is a one-cell table), so every cell's state and curve match bit for bit."""
     monkeypatch.delenv("NFX_TILE_TETS", raising=False)
     monkeypatch.delenv("NFX_TET_KERNEL", raising=False)
     cells = small_population()
@@ -37,8 +38,32 @@ def test_batch_equals_cells_run_alone_bitwise(monkeypatch):
         w.configure(s, m, max_rows=10)
         s.step(250)
         s.record_now()
+        assert s.status() == 0, i
+        assert np.abs(s.curve()[:, 2]).max() > 0, i  # the cell touched the indenter
         assert np.array_equal(b.points(i), s.points()), i
         assert np.array_equal(b.curve(i), s.curve()), i
+        s.close()
+    b.close()
+
+
+def test_batch_on_demand_readout_per_cell():
+    """nfx_batch_indenter_force gives every cell's force, equal to the cell run alone."""
+    cells = small_population()
+    meshes = [w.mesh() for w in cells]
+    b = Batch(0, tile_tets=128)
+    for w, m in zip(cells, meshes):
+        w.add_to_batch(b, m)
+    b.set_record(1, 50, 10)
+    b.finalize()
+    b.step(120)
+    got = b.indenter_force(1)
+    assert got.shape == (4,)
+    assert np.all(b.indenter_force(3) == 0.0)  # no cell has a fourth contact
+    for i, (w, m) in enumerate(zip(cells, meshes)):
+        s = CellSim(0)
+        w.configure(s, m, max_rows=10)
+        s.step(120)
+        assert got[i] == s.indenter_force(1), i
         s.close()
     b.close()
 

@@ -63,3 +63,22 @@ def test_workload_definitions():
     assert l.radius == 64 and l.material == "mr_vp" and l.indenter == "sphere" and l.sphere_radius == 16
     par = l.vp_params()
     assert par[0] == 1e-3 and par[1] == 2e-4 and par[5] == pytest.approx(4e-3)
+
+
+@pytest.mark.parametrize("R", [2.6, 3.6, 3.811, 6.5, 13.3, 17.0])
+def test_batched_walls_start_tangent(R):
+    """With d0 = None the substrate and the sphere start touching the bottom and top nodes and
+    no node starts inside either wall, for integer and non-integer radii."""
+    from nofluidx3d_gb300.workloads import batched_cells
+
+    w = batched_cells(1, seed=3)[0].with_(radius=R, sphere_radius=R / 4.0)
+    m = w.mesh()
+    sub, sph = w.contacts(m)
+    p = m.points
+    assert sub["p0"] == pytest.approx(p[:, 1].min())
+    assert sph["p0"] - sph["radius"] == pytest.approx(p[:, 1].max())
+    assert np.all(p[:, 1] >= sub["p0"] - 1e-12)
+    d = np.linalg.norm(p - np.array([0.0, sph["p0"], 0.0]), axis=1)
+    assert d.min() >= sph["radius"] - 1e-12
+    with pytest.raises(ValueError):
+        w.contacts()  # d0 = None needs the mesh
