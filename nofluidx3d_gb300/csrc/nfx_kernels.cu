@@ -3,18 +3,22 @@
 // One time step is two kernels:
 //   k_tet_pass  — one CTA per tile of tetrahedra: stage the tile's nodes (displacement hi/lo)
 //                 in shared memory, evaluate each tetra's material law in registers
-//                 (tetra.cl:14-182 or InteractionFiniteStrainViscoplastic.cl:1-220), sum the 12
-//                 nodal force components per tetra into shared-memory node slots, then flush one
-//                 float4 atomic per distinct node to the force accumulator. This replaces the
-//                 reference's 12 FP64 CAS loops per tetra (atomicAdd.cl:1-11).
+//                 (tetra.cl:14-182 or InteractionFiniteStrainViscoplastic.cl:1-220), write the
+//                 four corner forces to shared memory, sum them per distinct tile node in the
+//                 tile's fixed incidence order, and add each node sum to the force accumulator
+//                 as 64-bit fixed point (three integer atomics per tile node). This replaces
+//                 the reference's 12 FP64 CAS loops per tetra (atomicAdd.cl:1-11) and makes the
+//                 accumulated force independent of the order in which tiles finish.
 //   k_node_pass — one thread per node: accumulated element force + substrate/plane/sphere
 //                 contacts (Substrate.cl, Plane.cl, Sphere.cl), damped velocity Verlet
 //                 (VelocityVerlet.cl:1-36) with the displacement carried as float hi + lo,
 //                 zeroing of the accumulator, and on record steps the indenter-force readout of
-//                 Simulation.py:146-153 / :198-212 reduced with warp shuffles in a fixed order.
-// The kernel boundary is the step's only global barrier. Time t comes from device memory
-// (start of the captured chunk) plus the launch's offset, so a captured CUDA graph of G steps
-// can be replayed for any chunk.
+//                 Simulation.py:146-153 / :198-212 reduced per cell in a fixed order.
+// Both kernels read their parameters from a per-cell table in device memory (BatchDev): a single
+// simulation is a table of one cell, a batch many, and both run this same code. The kernel
+// boundary is the step's only global barrier. Time t comes from device memory (start of the
+// captured chunk) plus the launch's offset, so a captured CUDA graph of G steps can be replayed
+// for any chunk.
 #include <cuda_runtime.h>
 
 #include "nfx_internal.h"
@@ -509,7 +513,7 @@ __device__ __forceinline__ double node_step(const MeshDev& m, const StateDev& s,
 // last block to finish — the cell's block partials in index order, so the result is the same on
 // every run and does not depend on which other cells share the launch.
 #ifndef NFX_NODE_MIN_BLOCKS
-#define NFX_NODE_MIN_BLOCKS 1  // resident node-pass blocks per SM the register allocation must allow
+#define NFX_NODE_MIN_BLOCKS 4  // resident node-pass blocks per SM (64 registers; 4 cost 30 us less than 1 at R=64)
 #endif
 __global__ void __launch_bounds__(NODE_BLOCK, NFX_NODE_MIN_BLOCKS) k_node_pass(MeshDev m, StateDev s, BatchDev bd, int t_offset, int mode,
                                                           int readout_contact) {
