@@ -247,6 +247,48 @@ int nfx_batch_tuning(nfx_batch* batch, int* tiles, float* ms, int max_n, int* n)
 int nfx_indenter_force_noalloc(int device, int64_t np, const double* points_dev, int kind, double k, double radius,
                                double position, double* out_dev, void* stream);
 
+/* ------------------------------------------------------------------------------------------
+ * Surrogate MLP of the force-indentation curve. No counterpart in the reference (which has no
+ * learned part): material parameters -> curve samples, n_in -> width (x depth hidden layers,
+ * SiLU) -> n_out, BF16 weights and activations, FP32 accumulation (tensor-core MMAs), FP32
+ * master weights and AdamW. Arrays are host pointers, row-major, FP32.
+ * Parameter layout (nfx_mlp_set_params/get_params/get_grads): for each layer l in order,
+ * W_l [out_l x in_l] row-major, then b_l [out_l].
+ * ------------------------------------------------------------------------------------------ */
+typedef struct nfx_mlp nfx_mlp;
+/* n_in 1..16; width a multiple of 16 up to 1024; depth 1..7 hidden layers; n_out a multiple of
+ * 8 up to 1024; max_batch rows per call. Parameters start at zero: set them before use. */
+int nfx_mlp_create(int device, int n_in, int width, int depth, int n_out, int64_t max_batch, nfx_mlp** out);
+int nfx_mlp_destroy(nfx_mlp* mlp);
+int nfx_mlp_num_params(nfx_mlp* mlp, int64_t* n);
+/* Sets the FP32 master parameters (and their BF16 copies); resets the AdamW moments and step. */
+int nfx_mlp_set_params(nfx_mlp* mlp, const float* params);
+int nfx_mlp_get_params(nfx_mlp* mlp, float* params);
+/* Gradients of the last nfx_mlp_backward / training step, same layout as the parameters. */
+int nfx_mlp_get_grads(nfx_mlp* mlp, float* grads);
+/* y[batch x n_out] = f(x[batch x n_in]). */
+int nfx_mlp_forward(nfx_mlp* mlp, const float* x, int64_t batch, float* y);
+/* Loss L = scale * sum_b w_b * ||f(x_b) - target_b||^2 (w = 1 when weight is NULL): per-row
+ * losses w_b * ||.||^2 into loss[batch] (nullable), the parameter gradients of L kept for
+ * nfx_mlp_adamw / nfx_mlp_get_grads, and dL/dx into dx[batch x n_in] when dx is not NULL. */
+int nfx_mlp_backward(nfx_mlp* mlp, const float* x, const float* target, const float* weight, int64_t batch,
+                     float scale, float* loss, float* dx);
+/* One AdamW update of every parameter from the stored gradients (decoupled weight decay on the
+ * weights, not on the biases). */
+int nfx_mlp_adamw(nfx_mlp* mlp, float lr, float beta1, float beta2, float eps, float weight_decay);
+/* steps minibatch steps over a dataset of n rows uploaded once (x[n x n_in], target[n x n_out],
+ * weight[n] nullable): PCG32-shuffled epochs (seed), mean weighted squared-error loss, AdamW with
+ * a cosine learning rate from hp[0] to hp[5]; hp = {lr, beta1, beta2, eps, weight_decay, lr_min}.
+ * losses[steps] (nullable) receives each step's mean loss. */
+int nfx_mlp_train(nfx_mlp* mlp, const float* x, const float* target, const float* weight, int64_t n, int64_t batch,
+                  int64_t steps, const float* hp, uint64_t seed, float* losses);
+/* Inverse problem: Adam on the inputs of `batch` rows to minimise w_b * ||f(x_b) - target_b||^2;
+ * only inputs with free_mask[k] != 0 move, all stay in [lo[k], hi[k]]. x is updated in place;
+ * loss[batch] (nullable) gets the final per-row loss. hp = {lr, beta1, beta2, eps}. */
+int nfx_mlp_fit_inputs(nfx_mlp* mlp, float* x, const float* target, const float* weight, int64_t batch,
+                       const unsigned char* free_mask, const float* lo, const float* hi, int64_t steps,
+                       const float* hp, float* loss);
+
 #ifdef __cplusplus
 }
 #endif

@@ -87,6 +87,17 @@ _SIGS = {
     "nfx_batch_status": ([_vp, C.POINTER(C.c_uint32), C.c_int], C.c_int),
     "nfx_batch_info": ([_vp, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64), C.POINTER(C.c_int)], C.c_int),
     "nfx_batch_tuning": ([_vp, _vp, _vp, C.c_int, C.POINTER(C.c_int)], C.c_int),
+    "nfx_mlp_create": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _i64, C.POINTER(_vp)], C.c_int),
+    "nfx_mlp_destroy": ([_vp], C.c_int),
+    "nfx_mlp_num_params": ([_vp, C.POINTER(_i64)], C.c_int),
+    "nfx_mlp_set_params": ([_vp, _vp], C.c_int),
+    "nfx_mlp_get_params": ([_vp, _vp], C.c_int),
+    "nfx_mlp_get_grads": ([_vp, _vp], C.c_int),
+    "nfx_mlp_forward": ([_vp, _vp, _i64, _vp], C.c_int),
+    "nfx_mlp_backward": ([_vp, _vp, _vp, _vp, _i64, C.c_float, _vp, _vp], C.c_int),
+    "nfx_mlp_adamw": ([_vp, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float], C.c_int),
+    "nfx_mlp_train": ([_vp, _vp, _vp, _vp, _i64, _i64, _i64, _vp, C.c_uint64, _vp], C.c_int),
+    "nfx_mlp_fit_inputs": ([_vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp], C.c_int),
 }
 
 

@@ -20,7 +20,7 @@ BUILD_DIR = PKG / "_build"
 LIB_NAME = "libnfx.so"
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-SOURCES = ["nfx_kernels.cu", "nfx_noalloc.cu", "nfx_api.cpp", "nfx_mesh.cpp", "nfx_batch.cpp"]
+SOURCES = ["nfx_kernels.cu", "nfx_noalloc.cu", "nfx_mlp.cu", "nfx_api.cpp", "nfx_mesh.cpp", "nfx_batch.cpp"]
 HEADERS = ["nfx_internal.h", "nfx_math.cuh"]
 
 

@@ -65,7 +65,7 @@ struct nfx_sim {
     long long table_cap[MAX_CONTACTS] = {0, 0, 0, 0};
     // fixed-size control block
     unsigned* d_status = nullptr;
-    long long* d_time = nullptr;
+    StepClock* d_clock = nullptr;
     unsigned* d_counter = nullptr;
     double* d_force_out = nullptr;
     double* d_curve = nullptr;
@@ -104,7 +104,7 @@ void free_mesh(nfx_sim* s) {
     StateDev keep = s->st;
     s->st = StateDev{};
     s->st.status = keep.status;
-    s->st.time = keep.time;
+    s->st.clock = keep.clock;
     s->st.force_out = keep.force_out;
     s->d_node_user = nullptr;
     s->d_stage = nullptr;
@@ -170,7 +170,7 @@ int enqueue_steps(nfx_sim* s, int n) {
         CUDA_TRY(launch_elem(s, k));
         CUDA_TRY(launch_nodes(s, k, NODE_UPDATE, -1));
     }
-    CUDA_TRY(launch_advance_time(s->st, n, s->stream));
+    CUDA_TRY(launch_advance_time(s->st, n, s->fields_every, s->record_every, s->stream));
     return NFX_OK;
 }
 
@@ -237,17 +237,17 @@ int nfx_create(int device, nfx_sim** out) {
     if ((rc = set_device(s)) != NFX_OK) { delete s; return rc; }
     e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { delete s; return fail(NFX_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)); }
-    if ((rc = dalloc(s, &s->d_status, 1, nullptr)) != NFX_OK || (rc = dalloc(s, &s->d_time, 1, nullptr)) != NFX_OK ||
+    if ((rc = dalloc(s, &s->d_status, 1, nullptr)) != NFX_OK || (rc = dalloc(s, &s->d_clock, 1, nullptr)) != NFX_OK ||
         (rc = dalloc(s, &s->d_counter, 1, nullptr)) != NFX_OK || (rc = dalloc(s, &s->d_force_out, 1, nullptr)) != NFX_OK ||
         (rc = dalloc(s, &s->d_cell, 1, nullptr)) != NFX_OK) {
         nfx_destroy(s);
         return rc;
     }
     cudaMemsetAsync(s->d_status, 0, sizeof(unsigned), s->stream);
-    cudaMemsetAsync(s->d_time, 0, sizeof(long long), s->stream);
+    cudaMemsetAsync(s->d_clock, 0, sizeof(StepClock), s->stream);
     cudaMemsetAsync(s->d_counter, 0, sizeof(unsigned), s->stream);
     s->st.status = s->d_status;
-    s->st.time = s->d_time;
+    s->st.clock = s->d_clock;
     s->st.force_out = s->d_force_out;
     s->cell.record_contact = -1;
     s->cell.fix_a = s->cell.fix_b = -1;
@@ -279,7 +279,7 @@ int nfx_destroy(nfx_sim* s) {
     }
     if (s->d_curve) cudaFree(s->d_curve);
     if (s->d_status) cudaFree(s->d_status);
-    if (s->d_time) cudaFree(s->d_time);
+    if (s->d_clock) cudaFree(s->d_clock);
     if (s->d_counter) cudaFree(s->d_counter);
     if (s->d_force_out) cudaFree(s->d_force_out);
     if (s->d_cell) cudaFree(s->d_cell);
@@ -350,7 +350,8 @@ int nfx_set_mesh(nfx_sim* s, int64_t np, int64_t nt, const double* points, const
     CUDA_TRY(cudaMemcpyAsync(s->d_node_user, nu.data(), nu.size() * sizeof(long long), cudaMemcpyHostToDevice, st));
     for (float4* z : {uh, ul, v, fo}) CUDA_TRY(cudaMemsetAsync(z, 0, (size_t)np * sizeof(float4), st));
     CUDA_TRY(cudaMemsetAsync(fa, 0, 3 * (size_t)np * sizeof(unsigned long long), st));
-    CUDA_TRY(cudaMemsetAsync(s->d_time, 0, sizeof(long long), st));
+    CUDA_TRY(cudaMemsetAsync(s->d_clock, 0, sizeof(StepClock), st));
+    CUDA_TRY(launch_advance_time(s->st, 0, s->fields_every, s->record_every, st));
     CUDA_TRY(cudaMemsetAsync(s->d_status, 0, sizeof(unsigned), st));
     CUDA_TRY(cudaStreamSynchronize(st));  // host vectors a/b/c/nu go out of scope
     s->mesh.np = (int)np;
@@ -535,6 +536,7 @@ int nfx_set_record(nfx_sim* s, int contact, int64_t every, int64_t max_rows) {
     s->fields_every = every > 0 ? every : 0;
     s->rows_written = 0;
     invalidate_graph(s);  // record settings and the curve buffer are kernel arguments
+    CUDA_TRY(launch_advance_time(s->st, 0, s->fields_every, s->record_every, s->stream));
     return NFX_OK;
 }
 
@@ -752,14 +754,15 @@ int nfx_profile_steps(nfx_sim* s, int64_t nsteps, float* tet_ms, float* node_ms)
     for (auto& e : ev) CUDA_TRY(cudaEventCreate(&e));
     const long long t_begin = s->time;
     cudaError_t err = cudaSuccess;
+    // one step per clock advance, so the step offset stays inside the clock's window
     for (int64_t k = 0; k < nsteps && err == cudaSuccess; k++) {
         cudaEventRecord(ev[3 * k], s->stream);
-        err = launch_elem(s, (int)k);
+        err = launch_elem(s, 0);
         cudaEventRecord(ev[3 * k + 1], s->stream);
-        if (err == cudaSuccess) err = launch_nodes(s, (int)k, NODE_UPDATE, -1);
+        if (err == cudaSuccess) err = launch_nodes(s, 0, NODE_UPDATE, -1);
         cudaEventRecord(ev[3 * k + 2], s->stream);
+        if (err == cudaSuccess) err = launch_advance_time(s->st, 1, s->fields_every, s->record_every, s->stream);
     }
-    if (err == cudaSuccess) err = launch_advance_time(s->st, nsteps, s->stream);
     if (err == cudaSuccess) err = cudaStreamSynchronize(s->stream);
     float a = 0.f, b = 0.f;
     for (int64_t k = 0; k < nsteps && err == cudaSuccess; k++) {

@@ -63,7 +63,7 @@ struct BatchDevice {
     StateDev st{};
     BatchDev bd{};
     int nblocks = 0;
-    long long* d_time = nullptr;
+    StepClock* d_clock = nullptr;
     unsigned* d_status = nullptr;
     cudaGraphExec_t graph = nullptr;
     void release() {
@@ -223,7 +223,7 @@ int build_device(nfx_batch* b, const std::vector<int>& which, int tile_tets, Bat
         (rc = balloc(A, &d_fa, 3 * (size_t)np)) || (rc = balloc(A, &d_part, nblocks)) || (rc = balloc(A, &d_fout, cells.size())) ||
         (rc = balloc(A, &d_cells, cells.size())) || (rc = balloc(A, &d_tc, ntiles)) || (rc = balloc(A, &d_bc, nblocks)) ||
         (rc = balloc(A, &d_cc, cells.size())) || (rc = balloc(A, &d_curves, 3 * rows * cells.size())) ||
-        (rc = balloc(A, &D.d_time, 1)) || (rc = balloc(A, &D.d_status, 1)))
+        (rc = balloc(A, &D.d_clock, 1)) || (rc = balloc(A, &D.d_status, 1)))
         return rc;
     if (b->model == MODEL_VP) {
         if ((rc = balloc(A, &d_pa, ntp)) || (rc = balloc(A, &d_pb, ntp)) || (rc = balloc(A, &d_pc, ntp)) ||
@@ -250,7 +250,7 @@ int build_device(nfx_batch* b, const std::vector<int>& which, int tile_tets, Bat
     BCUDA(cudaMemcpyAsync(d_bc, block_cell.data(), block_cell.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     BCUDA(cudaMemsetAsync(d_cc, 0, cells.size() * sizeof(unsigned), st));
     BCUDA(cudaMemsetAsync(d_curves, 0, 3 * rows * cells.size() * sizeof(double), st));
-    BCUDA(cudaMemsetAsync(D.d_time, 0, sizeof(long long), st));
+    BCUDA(cudaMemsetAsync(D.d_clock, 0, sizeof(StepClock), st));
     BCUDA(cudaMemsetAsync(D.d_status, 0, sizeof(unsigned), st));
     if (b->model == MODEL_VP) {
         BCUDA(cudaMemsetAsync(d_pa, 0, ntp * sizeof(float4), st));
@@ -287,7 +287,7 @@ int build_device(nfx_batch* b, const std::vector<int>& which, int tile_tets, Bat
     S.vp_c = d_pc;
     S.fields = d_fields;
     S.status = D.d_status;
-    S.time = D.d_time;
+    S.clock = D.d_clock;
     S.partials = d_part;
     S.force_out = d_fout;
     BatchDev& B = D.bd;
@@ -300,6 +300,8 @@ int build_device(nfx_batch* b, const std::vector<int>& which, int tile_tets, Bat
     B.max_rows = b->max_rows;
     B.fields_every = b->record_every;
     D.nblocks = (int)nblocks;
+    BCUDA(launch_advance_time(S, 0, B.fields_every, B.record_every, st));
+    BCUDA(cudaStreamSynchronize(st));
     return NFX_OK;
 }
 
@@ -308,7 +310,7 @@ int enqueue_batch_steps(nfx_batch* b, BatchDevice& D, int n) {
         BCUDA(launch_tet_pass(D.mesh, D.st, D.bd, b->model, k, b->stream));
         BCUDA(launch_node_pass(D.mesh, D.st, D.bd, D.nblocks, k, NODE_UPDATE, -1, b->stream));
     }
-    BCUDA(launch_advance_time(D.st, n, b->stream));
+    BCUDA(launch_advance_time(D.st, n, D.bd.fields_every, D.bd.record_every, b->stream));
     return NFX_OK;
 }
 

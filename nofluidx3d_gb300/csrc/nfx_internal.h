@@ -87,6 +87,18 @@ struct MeshDev {
     const float4* Xl;
 };
 
+// Device-side step clock: the simulation time at the start of the current chunk of launches and,
+// for the next CLOCK_WINDOW steps (t_offset 0 .. CLOCK_WINDOW-1), bitmasks of the steps that
+// write the per-tetra fields and of those that record a curve row. k_advance_time refreshes the
+// masks whenever it moves the time, so a step tests one bit instead of dividing 64-bit integers
+// on every thread. Every chunk of launches between two refreshes stays within the window.
+constexpr int CLOCK_WINDOW = 128;
+struct StepClock {
+    long long time;
+    unsigned fields_due[CLOCK_WINDOW / 32];  // bit k: (time + k + 1) % fields_every == 0
+    unsigned record_due[CLOCK_WINDOW / 32];  // bit k: (time + k) % record_every == 0
+};
+
 struct StateDev {
     float4* uh;     // displacement hi
     float4* ul;     // displacement lo
@@ -101,7 +113,7 @@ struct StateDev {
     float2* vp_c;   // entry 8, accumulated plastic strain
     float2* fields; // von Mises, pressure per tetra (viscoplastic model)
     unsigned* status;
-    long long* time;     // simulation time at the start of the current graph chunk
+    StepClock* clock;    // time at the start of the current chunk + schedule masks
     double* partials;    // one per node block, for the deterministic readout reduction
     double* force_out;   // per cell: result of an on-demand readout
 };
@@ -172,7 +184,9 @@ enum NodeMode : int { NODE_UPDATE = 0, NODE_READOUT_ROW = 1, NODE_READOUT_VALUE 
 // per cell into force_out[cell] without updating the state.
 cudaError_t launch_node_pass(const MeshDev& m, const StateDev& s, const BatchDev& b, int nblocks, int t_offset,
                              int mode, int readout_contact, cudaStream_t stream);
-cudaError_t launch_advance_time(const StateDev& s, long long n, cudaStream_t stream);
+// Advance the clock by n steps (n = 0: refresh the masks only) for the given schedules.
+cudaError_t launch_advance_time(const StateDev& s, long long n, long long fields_every, long long record_every,
+                                cudaStream_t stream);
 // Conversions between the user's layout (SoA doubles, user order) and the device state.
 cudaError_t launch_points_to_user(const MeshDev& m, const StateDev& s, const long long* node_user, double* out,
                                   cudaStream_t stream);

@@ -45,8 +45,9 @@ __device__ __forceinline__ double contact_pos(const ContactDev& c, long long t) 
 
 // One tetra: displacement differences from the tile's staged node data, the material law, the
 // viscoplastic state update (written back with evict-first stores), the four corner forces
-// into the shared corner-force slots 4*j .. 4*j+3.
-template <int MODEL>
+// into the shared corner-force slots k*TILE + j (corner-major, so a warp's stores are
+// contiguous and free of bank conflicts).
+template <int MODEL, int TILE>
 __device__ __forceinline__ void element_eval(int j, long long t, uchar4 lc, float4 da, float4 db, float2 dc,
                                              float4 pa, float4 pb, float2 pc, const float4* s_uh,
                                              const float4* s_ul, float4* s_cf, const StateDev& s,
@@ -95,19 +96,21 @@ __device__ __forceinline__ void element_eval(int j, long long t, uchar4 lc, floa
     }
     if (!(jm1 > -1.0f)) atomicOr(s.status, STATUS_INVERTED);
 #pragma unroll
-    for (int k = 0; k < 4; k++) s_cf[4 * j + k] = make_float4(f[k][0], f[k][1], f[k][2], 0.f);
+    for (int k = 0; k < 4; k++) s_cf[k * TILE + j] = make_float4(f[k][0], f[k][1], f[k][2], 0.f);
 }
 
 // One tile node: sum its corner forces in the tile's fixed incidence order and add the sum to
 // the global accumulator as 64-bit fixed point, so the total does not depend on the order in
-// which tiles finish.
+// which tiles finish. Incidence entries are 4*local tet + corner.
+template <int TILE>
 __device__ __forceinline__ void node_flush(uint2 node, const unsigned short* inc, const float4* s_cf,
                                            const StateDev& s, long long np) {
     const unsigned first = node.y >> 16, count = node.y & 0xffffu;
     if (count == 0) return;
     float fx = 0.f, fy = 0.f, fz = 0.f;
     for (unsigned q = 0; q < count; q++) {
-        const float4 c = s_cf[inc[first + q]];
+        const unsigned e = inc[first + q];
+        const float4 c = s_cf[(e & 3u) * TILE + (e >> 2)];
         fx += c.x;
         fy += c.y;
         fz += c.z;
@@ -121,11 +124,7 @@ __device__ __forceinline__ void node_flush(uint2 node, const unsigned short* inc
     atomicAdd(s.facc + 2 * np + node.x, (unsigned long long)__float2ll_rn(fz * FORCE_FIX_SCALE));
 }
 
-__device__ __forceinline__ bool fields_due(const StateDev& s, long long fields_every, int t_offset) {
-    if (fields_every <= 0) return false;
-    const long long tt = *s.time + t_offset;
-    return (tt + 1) % fields_every == 0;
-}
+__device__ __forceinline__ bool clock_bit(const unsigned* mask, int k) { return (mask[k >> 5] >> (k & 31)) & 1u; }
 
 // ------------------------------------------------------------------------------------------
 // Element pass, one CTA per tile (plain loads)
@@ -138,7 +137,7 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * 64))
     constexpr int NMAX = TILE < TILE_NODES_MAX ? TILE : TILE_NODES_MAX;
     __shared__ float4 s_uh[NMAX];
     __shared__ float4 s_ul[NMAX];
-    __shared__ float4 s_cf[4 * TILE];  // corner forces, slot 4*local tet + corner
+    __shared__ float4 s_cf[4 * TILE];  // corner forces, slot corner*TILE + local tet
     __shared__ ushort4 s_inc[TILE];    // the tile's incidence list
 
     const int b = blockIdx.x;
@@ -151,7 +150,7 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * 64))
     const int ntt = (int)(meta & 0xffffu);
     const int nn = (int)(meta >> 16);
     const bool act = j < ntt;
-    const bool wf = fields_due(s, bd.fields_every, t_offset);
+    const bool wf = clock_bit(s.clock->fields_due, t_offset);
 
     // Streaming per-tetra data (read once per step: evict-first) and the node list, issued for
     // every slot and entry without waiting for the meta word: padding is valid zeroed memory.
@@ -175,9 +174,9 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * 64))
     }
     const MaterialDev mat = bd.cells[bd.tile_cell ? __ldg(bd.tile_cell + b) : 0].mat;
     __syncthreads();
-    if (act) element_eval<MODEL>(j, t, lc, da, db, dc, pa, pb, pc, s_uh, s_ul, s_cf, s, mat, wf);
+    if (act) element_eval<MODEL, TILE>(j, t, lc, da, db, dc, pa, pb, pc, s_uh, s_ul, s_cf, s, mat, wf);
     __syncthreads();
-    if (j < nn) node_flush(node, reinterpret_cast<const unsigned short*>(s_inc), s_cf, s, m.np);
+    if (j < nn) node_flush<TILE>(node, reinterpret_cast<const unsigned short*>(s_inc), s_cf, s, m.np);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -332,7 +331,7 @@ __global__ void __launch_bounds__(TILE) k_tet_pass_pipe(MeshDev m, StateDev s, B
     const int j = threadIdx.x;
     const int G = gridDim.x;
     const int first = blockIdx.x;
-    const bool wf = fields_due(s, bd.fields_every, t_offset);
+    const bool wf = clock_bit(s.clock->fields_due, t_offset);
     const MaterialDev mat = bd.cells[0].mat;
     if (first >= m.ntiles) return;
 
@@ -381,7 +380,7 @@ __global__ void __launch_bounds__(TILE) k_tet_pass_pipe(MeshDev m, StateDev s, B
                 pb = vpb[j];
                 pc = vpc[j];
             }
-            element_eval<MODEL>(j, (long long)h.tb + j, reinterpret_cast<const uchar4*>(st + StageLayout::LCONN)[j],
+            element_eval<MODEL, TILE>(j, (long long)h.tb + j, reinterpret_cast<const uchar4*>(st + StageLayout::LCONN)[j],
                                 reinterpret_cast<const float4*>(st + StageLayout::DMI_A)[j],
                                 reinterpret_cast<const float4*>(st + StageLayout::DMI_B)[j],
                                 reinterpret_cast<const float2*>(st + StageLayout::DMI_C)[j], pa, pb, pc,
@@ -391,7 +390,7 @@ __global__ void __launch_bounds__(TILE) k_tet_pass_pipe(MeshDev m, StateDev s, B
         __syncthreads();  // corner forces complete
         if (j < h.nn) {
             const uint2 node = reinterpret_cast<const uint2*>(st + StageLayout::NODES)[h.noff + j];
-            node_flush(node, reinterpret_cast<const unsigned short*>(st + StageLayout::INC), s_cf, s, m.np);
+            node_flush<TILE>(node, reinterpret_cast<const unsigned short*>(st + StageLayout::INC), s_cf, s, m.np);
         }
         __syncthreads();  // stage `cur` and the corner forces are free again
         if (j == 0 && tile + 2 * G < m.ntiles) {
@@ -464,7 +463,7 @@ __device__ __forceinline__ double contact_force(const ContactDev& c, double w, c
 // One node: element force from the fixed-point accumulator, the contacts in order (returns the
 // readout value -f_y of contact rc), and in update mode the damped velocity-Verlet step with the
 // displacement carried as hi + lo, the FIXED_TOP_BOTTOM pin, and the accumulator reset.
-__device__ __forceinline__ double node_step(const MeshDev& m, const StateDev& s, int i, long long t,
+__device__ __forceinline__ double node_step(const MeshDev& m, const StateDev& s, int i, const double* wall,
                                            const ContactDev* cs, int nc, int rc, float vv_a, float vv_hb,
                                            float vv_dm, int fix_a, int fix_b, bool update) {
     const long long np = m.np;
@@ -475,8 +474,7 @@ __device__ __forceinline__ double node_step(const MeshDev& m, const StateDev& s,
     float4 uh = s.uh[i], ul = s.ul[i];
     double ro = 0.0;
     for (int c = 0; c < nc; c++) {
-        const double w = contact_pos(cs[c], t);
-        const double fy = contact_force(cs[c], w, xh, m.Xl + i, uh, ul, f);
+        const double fy = contact_force(cs[c], wall[c], xh, m.Xl + i, uh, ul, f);
         if (c == rc) ro = -fy;
     }
     if (update) {
@@ -518,11 +516,16 @@ __device__ __forceinline__ double node_step(const MeshDev& m, const StateDev& s,
 __global__ void __launch_bounds__(NODE_BLOCK, NFX_NODE_MIN_BLOCKS) k_node_pass(MeshDev m, StateDev s, BatchDev bd, int t_offset, int mode,
                                                           int readout_contact) {
     __shared__ double s_w[NODE_BLOCK / 32];
+    __shared__ double s_wall[MAX_CONTACTS];
     __shared__ int s_last;
     const int cell = bd.block_cell ? __ldg(bd.block_cell + blockIdx.x) : 0;
     const CellDev& C = bd.cells[cell];
     const int i = blockIdx.x * NODE_BLOCK + threadIdx.x;
-    const long long t = *s.time + t_offset;
+    const long long t = s.clock->time + t_offset;
+    // the cell's contact positions at time t, once per block (FP64 and table lookups stay off the
+    // per-node path)
+    if (threadIdx.x < C.n_contacts) s_wall[threadIdx.x] = contact_pos(C.c[threadIdx.x], t);
+    __syncthreads();
     int rc;
     bool rec;
     long long row = 0;
@@ -531,7 +534,7 @@ __global__ void __launch_bounds__(NODE_BLOCK, NFX_NODE_MIN_BLOCKS) k_node_pass(M
         rec = true;
     } else {
         rc = C.record_contact;
-        rec = rc >= 0 && bd.record_every > 0 && (t % bd.record_every) == 0;
+        rec = rc >= 0 && clock_bit(s.clock->record_due, t_offset);
         if (rec) {
             row = t / bd.record_every;
             if (row >= bd.max_rows) {
@@ -542,7 +545,7 @@ __global__ void __launch_bounds__(NODE_BLOCK, NFX_NODE_MIN_BLOCKS) k_node_pass(M
     }
     double ro = 0.0;
     if (i < C.node_end)
-        ro = node_step(m, s, i, t, C.c, C.n_contacts, rc, C.vv_a, C.vv_hb, C.vv_dm, C.fix_a, C.fix_b,
+        ro = node_step(m, s, i, s_wall, C.c, C.n_contacts, rc, C.vv_a, C.vv_hb, C.vv_dm, C.fix_a, C.fix_b,
                        mode == NODE_UPDATE);
     if (!rec) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -576,14 +579,29 @@ __global__ void __launch_bounds__(NODE_BLOCK, NFX_NODE_MIN_BLOCKS) k_node_pass(M
         } else {
             double* r = bd.curves + 3 * ((long long)cell * bd.max_rows + row);
             r[0] = (double)t;
-            r[1] = contact_pos(C.c[rc], 0) - contact_pos(C.c[rc], t);
+            r[1] = contact_pos(C.c[rc], 0) - s_wall[rc];
             r[2] = tot;
         }
         bd.cell_counter[cell] = 0u;
     }
 }
 
-__global__ void k_advance_time(long long* time, long long n) { *time += n; }
+// One block of CLOCK_WINDOW threads: thread k evaluates step time + k of the next window.
+__global__ void __launch_bounds__(CLOCK_WINDOW) k_advance_time(StepClock* c, long long n, long long fields_every,
+                                                               long long record_every) {
+    const int k = threadIdx.x;
+    const long long t0 = c->time + n;
+    const long long t = t0 + k;
+    const bool f = fields_every > 0 && (t + 1) % fields_every == 0;
+    const bool r = record_every > 0 && t % record_every == 0;
+    const unsigned fm = __ballot_sync(0xffffffffu, f), rm = __ballot_sync(0xffffffffu, r);
+    __syncthreads();  // every thread has read the old time
+    if ((k & 31) == 0) {
+        c->fields_due[k >> 5] = fm;
+        c->record_due[k >> 5] = rm;
+    }
+    if (k == 0) c->time = t0;
+}
 
 // ------------------------------------------------------------------------------------------
 // Layout conversions (user order, SoA doubles) <-> device state
@@ -726,8 +744,9 @@ cudaError_t launch_node_pass(const MeshDev& m, const StateDev& s, const BatchDev
     return cudaGetLastError();
 }
 
-cudaError_t launch_advance_time(const StateDev& s, long long n, cudaStream_t st) {
-    k_advance_time<<<1, 1, 0, st>>>(s.time, n);
+cudaError_t launch_advance_time(const StateDev& s, long long n, long long fields_every, long long record_every,
+                                cudaStream_t st) {
+    k_advance_time<<<1, CLOCK_WINDOW, 0, st>>>(s.clock, n, fields_every, record_every);
     return cudaGetLastError();
 }
 
