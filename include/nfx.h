@@ -189,6 +189,9 @@ int nfx_batch_create(int device, int tile_tets, nfx_batch** out);
 int nfx_batch_destroy(nfx_batch* batch);
 /* Adds a cell (layouts as nfx_set_mesh); *cell receives its index. */
 int nfx_batch_add_cell(nfx_batch* batch, int64_t np, int64_t nt, const double* points, const uint32_t* tets, int* cell);
+/* Adds a cell with the same mesh as cell `src` (no copy of the arrays; the plan is built once
+ * for all cells sharing a mesh). Material, contacts and integrator are set per cell as usual. */
+int nfx_batch_add_cell_like(nfx_batch* batch, int src, int* cell);
 /* Per-cell material, as nfx_set_tetra / nfx_set_viscoplastic. */
 int nfx_batch_set_tetra(nfx_batch* batch, int cell, int model, double youngs_modulus, double poisson_ratio,
                         double mooney_rivlin_ratio);

@@ -71,6 +71,7 @@ _SIGS = {
     "nfx_batch_create": ([C.c_int, C.c_int, C.POINTER(_vp)], C.c_int),
     "nfx_batch_destroy": ([_vp], C.c_int),
     "nfx_batch_add_cell": ([_vp, _i64, _i64, _vp, _vp, C.POINTER(C.c_int)], C.c_int),
+    "nfx_batch_add_cell_like": ([_vp, C.c_int, C.POINTER(C.c_int)], C.c_int),
     "nfx_batch_set_tetra": ([_vp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double], C.c_int),
     "nfx_batch_set_viscoplastic": ([_vp, C.c_int, _vp], C.c_int),
     "nfx_batch_add_contact": ([_vp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,

@@ -236,6 +236,13 @@ class Batch:
         self.cells.append((np_, nt))
         return cid.value
 
+    def add_cell_like(self, src: int) -> int:
+        """A new cell with the same mesh as cell `src` (shared, not copied)."""
+        cid = C.c_int(-1)
+        check(self._L.nfx_batch_add_cell_like(self._h, int(src), C.byref(cid)))
+        self.cells.append(self.cells[src])
+        return cid.value
+
     def set_tetra(self, cell: int, model: int, youngs: float, poisson: float, mr_ratio: float = 1.0) -> None:
         check(self._L.nfx_batch_set_tetra(self._h, int(cell), int(model), float(youngs), float(poisson), float(mr_ratio)))
 

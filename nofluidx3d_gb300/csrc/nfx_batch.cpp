@@ -9,6 +9,8 @@
 
 #include <algorithm>
 #include <atomic>
+#include <map>
+#include <memory>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -43,15 +45,16 @@ int bfail(int code, const std::string& msg) {
 
 struct CellHost {
     int64_t np = 0, nt = 0;
-    std::vector<double> points;   // 3*np SoA
+    std::vector<double> points;   // 3*np SoA (empty when the mesh is another cell's)
     std::vector<uint32_t> tets;   // 4*nt SoA
+    int mesh_src = -1;            // cell whose mesh this cell shares, -1: its own
     MaterialDev mat{};
     bool has_mat = false;
     int n_contacts = 0;
     ContactDev c[MAX_CONTACTS]{};
     double xi = 0.005;
     bool fix_top_bottom = false;
-    MeshPlan plan;
+    std::shared_ptr<MeshPlan> plan;  // shared by every cell with the same mesh
     // placement in the concatenated arrays
     int64_t node_base = 0, tet_base = 0, tile_base = 0, block_base = 0, nblocks = 0;
 };
@@ -105,25 +108,41 @@ int balloc(std::vector<void*>& owner, T** p, size_t count) {
     return NFX_OK;
 }
 
-// Build the plans of the given cells with the given tile size on host threads.
+int mesh_owner(const nfx_batch* b, int cell) {
+    const int s = b->cells[cell].mesh_src;
+    return s < 0 ? cell : s;
+}
+
+// Build the plans of the given cells with the given tile size on host threads: one plan per
+// distinct mesh, shared by every cell that uses it.
 int build_plans(nfx_batch* b, const std::vector<int>& which, int tile_tets) {
-    std::vector<std::string> errs(which.size());
+    std::vector<int> owners;
+    for (int k : which) owners.push_back(mesh_owner(b, k));
+    std::sort(owners.begin(), owners.end());
+    owners.erase(std::unique(owners.begin(), owners.end()), owners.end());
+    std::vector<std::shared_ptr<MeshPlan>> plans(owners.size());
+    std::vector<std::string> errs(owners.size());
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
     std::vector<std::thread> pool;
     std::atomic<size_t> next{0};
     auto work = [&]() {
         for (;;) {
             const size_t k = next.fetch_add(1);
-            if (k >= which.size()) return;
-            CellHost& c = b->cells[which[k]];
-            if (!build_mesh_plan(c.np, c.nt, c.points.data(), c.tets.data(), tile_tets, c.plan, errs[k]))
-                errs[k] = "cell " + std::to_string(which[k]) + ": " + errs[k];
+            if (k >= owners.size()) return;
+            const CellHost& c = b->cells[owners[k]];
+            plans[k] = std::make_shared<MeshPlan>();
+            if (!build_mesh_plan(c.np, c.nt, c.points.data(), c.tets.data(), tile_tets, *plans[k], errs[k]))
+                errs[k] = "cell " + std::to_string(owners[k]) + ": " + errs[k];
         }
     };
-    for (unsigned t = 0; t < std::min<size_t>(hw, which.size()); t++) pool.emplace_back(work);
+    for (unsigned t = 0; t < std::min<size_t>(hw, owners.size()); t++) pool.emplace_back(work);
     for (auto& t : pool) t.join();
     for (auto& e : errs)
         if (!e.empty()) return bfail(NFX_ERR_ARG, e);
+    for (int k : which) {
+        const size_t o = std::lower_bound(owners.begin(), owners.end(), mesh_owner(b, k)) - owners.begin();
+        b->cells[k].plan = plans[o];
+    }
     return NFX_OK;
 }
 
@@ -139,10 +158,10 @@ int build_device(nfx_batch* b, const std::vector<int>& which, int tile_tets, Bat
         c.block_base = nblocks;
         c.nblocks = (c.np + NODE_BLOCK - 1) / NODE_BLOCK;
         np += c.nblocks * NODE_BLOCK;  // whole blocks per cell
-        nt += c.plan.nslots;  // tetra slots (whole tiles)
-        ntiles += c.plan.ntiles;
+        nt += c.plan->nslots;  // tetra slots (whole tiles)
+        ntiles += c.plan->ntiles;
         nblocks += c.nblocks;
-        ntn += (int64_t)c.plan.tile_nodes.size() / 2;
+        ntn += (int64_t)c.plan->tile_nodes.size() / 2;
     }
     if (np > 0x7fffffff || nt > 0x7fffffff) return bfail(NFX_ERR_ARG, "batch too large");
     const size_t ntp = (size_t)nt + ARRAY_PAD;
@@ -157,7 +176,7 @@ int build_device(nfx_batch* b, const std::vector<int>& which, int tile_tets, Bat
     int64_t tn_pos = 0;
     for (size_t k = 0; k < which.size(); k++) {
         CellHost& c = b->cells[which[k]];
-        const MeshPlan& P = c.plan;
+        const MeshPlan& P = *c.plan;
         for (int64_t t = 0; t < P.ntiles; t++) {
             tile_tet_begin[c.tile_base + t] = (int)(c.tet_base + P.tile_tet_begin[t]);
             tile_node_begin[c.tile_base + t] = (int)(tn_pos + P.tile_node_begin[t]);
@@ -464,6 +483,19 @@ int nfx_batch_add_cell(nfx_batch* b, int64_t np, int64_t nt, const double* point
     return NFX_OK;
 }
 
+int nfx_batch_add_cell_like(nfx_batch* b, int src, int* cell) {
+    int rc;
+    if ((rc = check_cell(b, src)) != NFX_OK) return rc;
+    if (b->finalized) return bfail(NFX_ERR_STATE, "batch already finalized");
+    CellHost c;
+    c.np = b->cells[src].np;
+    c.nt = b->cells[src].nt;
+    c.mesh_src = mesh_owner(b, src);
+    b->cells.push_back(std::move(c));
+    if (cell) *cell = (int)b->cells.size() - 1;
+    return NFX_OK;
+}
+
 int nfx_batch_set_tetra(nfx_batch* b, int cell, int model, double E, double nu, double mr) {
     int rc;
     if ((rc = check_cell(b, cell)) != NFX_OK) return rc;
@@ -570,12 +602,13 @@ int nfx_batch_finalize(nfx_batch* b) {
     if ((rc = build_device(b, all, tile, b->dev)) != NFX_OK) return rc;
     // only the maps for readback are kept on the host
     for (auto& c : b->cells) {
-        c.plan.lconn = {};
-        c.plan.tile_inc = {};
-        c.plan.dmi = {};
-        c.plan.tile_nodes = {};
-        c.plan.Xh = {};
-        c.plan.Xl = {};
+        MeshPlan& P = *c.plan;
+        P.lconn = {};
+        P.tile_inc = {};
+        P.dmi = {};
+        P.tile_nodes = {};
+        P.Xh = {};
+        P.Xl = {};
         c.points = {};
         c.tets = {};
     }
@@ -675,7 +708,7 @@ int nfx_batch_get_points(nfx_batch* b, int cell, double* out) {
     BCUDA(cudaMemcpyAsync(ul.data(), b->dev.st.ul + off, np * sizeof(float4), cudaMemcpyDeviceToHost, b->stream));
     BCUDA(cudaStreamSynchronize(b->stream));
     for (size_t i = 0; i < np; i++) {
-        const int64_t u = c.plan.node_user[i];
+        const int64_t u = c.plan->node_user[i];
         for (int d = 0; d < 3; d++)
             out[d * np + u] = ((double)xh[4 * i + d] + (double)xl[4 * i + d]) + ((double)uh[4 * i + d] + (double)ul[4 * i + d]);
     }

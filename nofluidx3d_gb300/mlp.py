@@ -73,9 +73,14 @@ class MLP:
         return out
 
     def forward(self, x) -> np.ndarray:
+        """f(x) for any number of rows (in chunks of max_batch)."""
         x = _f32(x).reshape(-1, self.n_in)
         y = np.empty((x.shape[0], self.n_out), np.float32)
-        check(self._L.nfx_mlp_forward(self._h, _ptr(x), x.shape[0], _ptr(y)))
+        for a in range(0, x.shape[0], self.max_batch):
+            xa = np.ascontiguousarray(x[a:a + self.max_batch])
+            ya = np.empty((xa.shape[0], self.n_out), np.float32)
+            check(self._L.nfx_mlp_forward(self._h, _ptr(xa), xa.shape[0], _ptr(ya)))
+            y[a:a + xa.shape[0]] = ya
         return y
 
     def backward(self, x, target, weight=None, scale: float = 1.0, want_dx: bool = False):

@@ -119,10 +119,11 @@ class Workload:
         sim.set_record(self.record_contact, self.record_every, rows)
         return m
 
-    def add_to_batch(self, batch, mesh: CellMesh | None = None) -> int:
-        """Add this cell (mesh, material, contacts, integrator) to a core.Batch; returns its index."""
+    def add_to_batch(self, batch, mesh: CellMesh | None = None, like: int | None = None) -> int:
+        """Add this cell (mesh, material, contacts, integrator) to a core.Batch; returns its index.
+        like: index of a cell already in the batch whose mesh (which must be `mesh`) is shared."""
         m = mesh if mesh is not None else self.mesh()
-        cell = batch.add_cell(m.points, m.tets)
+        cell = batch.add_cell(m.points, m.tets) if like is None else batch.add_cell_like(like)
         if self.material == "mr_vp":
             batch.set_viscoplastic(cell, self.vp_params())
         else:

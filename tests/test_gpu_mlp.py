@@ -104,7 +104,7 @@ def test_fit_inputs_recovers_hidden_inputs(net):
     x0[:, 5] = x_true[:, 5]  # one input known (fixed), the rest fitted
     mask = np.array([1, 1, 1, 1, 1, 0], bool)
     lo, hi = -np.ones(6, np.float32), np.ones(6, np.float32)
-    _, loss0 = m.backward(x0, target, want_dx=True)
+    loss0 = m.backward(x0, target)
     x, loss = m.fit_inputs(x0, target, mask, lo, hi, steps=600, lr=2e-2)
     assert np.all(x[:, 5] == x_true[:, 5])
     assert np.all(x <= 1) and np.all(x >= -1)
