@@ -13,8 +13,10 @@ Inverse fit: given a measured curve and the known indenter radius, find the five
 inputs. The plain method is a batched Levenberg-Marquardt on the simulator (finite-difference
 Jacobians, every evaluation a full simulation). The surrogate-assisted method proposes inputs by
 gradient descent through the network (many starts per target, no simulation), has the simulator
-verify each proposal, and refines with the same Levenberg-Marquardt where the verified curve
-still improves. The simulator is the judge of every reported error.
+verify each proposal, and refines it by defect correction (output space mapping): the target is
+shifted by the simulator-minus-network difference at the current point and the network's inputs
+are refitted to the shifted target, one verifying simulation per iteration, for as long as the
+simulated error keeps improving. The simulator is the judge of every reported error.
 
 The reference has no learned part; curves come from the batched simulator (core.Batch), whose
 cells evolve bit for bit as the plain path (core.CellSim) runs them alone.
@@ -246,7 +248,9 @@ class Surrogate:
         err = curve_error(self.predict(P), flat_t).reshape(n, starts)
         k = np.argmin(err, axis=1)
         best_u = flat_u.reshape(n, starts, N_IN)[np.arange(n), k]
-        return from_unit(best_u, self.proto)
+        out = from_unit(best_u, self.proto)
+        out[:, 5] = Rs  # exactly the known radius (the unit coordinate went through float32)
+        return out
 
 
 def _he_init(n_in: int, width: int, depth: int, n_out: int, seed: int) -> np.ndarray:
@@ -270,14 +274,14 @@ class FitResult:
     seconds: float = 0.0          # wall time (simulations, network calls and host work)
 
 
-def lm_fit(targets: np.ndarray, start: np.ndarray, proto: Protocol, max_iter: int = 15, h: float = 0.02,
+def lm_fit(targets: np.ndarray, start: np.ndarray, proto: Protocol, max_iter: int = 30, h: float = 0.02,
            lam0: float = 1e-2, rtol: float = 1e-3, start_curves: np.ndarray | None = None,
            stats: SimStats | None = None, simulate=None) -> FitResult:
     """Batched Levenberg-Marquardt on the simulator over the five material inputs in unit
     coordinates (the indenter radius stays as in `start`). Each iteration of each active target
     costs 5 simulations for a forward-difference Jacobian and 1 for the trial point; a target
-    stops when an accepted step improves its error by less than rtol relative, or after two
-    rejected steps in a row. start_curves (simulated curves at `start`, if already known) saves
+    stops when an accepted step improves its error by less than rtol relative, or after four
+    rejected steps in a row (the damping grows 4x per rejection). start_curves (simulated curves at `start`, if already known) saves
     the first evaluation. simulate(params, proto, stats) -> curves defaults to simulate_curves."""
     sim = simulate if simulate is not None else simulate_curves
     t0 = time.perf_counter()
@@ -285,10 +289,17 @@ def lm_fit(targets: np.ndarray, start: np.ndarray, proto: Protocol, max_iter: in
     n = T.shape[0]
     tn = np.maximum(np.linalg.norm(T, axis=1), 1e-300)
     u = to_unit(start, proto)
+    radius = np.asarray(start, np.float64).reshape(-1, N_IN)[:, 5].copy()
+
+    def phys(uu, rows):  # unit -> physical with the known indenter radius kept exact
+        q = from_unit(uu, proto)
+        q[:, 5] = radius[rows]
+        return q
+
     sims = np.zeros(n, np.int64)
     its = np.zeros(n, np.int64)
     if start_curves is None:
-        F = sim(from_unit(u, proto), proto, stats)
+        F = sim(phys(u, np.arange(n)), proto, stats)
         sims += 1
     else:
         F = np.asarray(start_curves, np.float64).copy()
@@ -307,7 +318,7 @@ def lm_fit(targets: np.ndarray, start: np.ndarray, proto: Protocol, max_iter: in
         U = np.repeat(u[idx][None], free.size, axis=0)               # [5, m, 6]
         for q, j in enumerate(free):
             U[q, :, j] += steps[:, q]
-        FJ = sim(from_unit(U.reshape(-1, N_IN), proto), proto, stats).reshape(free.size, m, -1)
+        FJ = sim(phys(U.reshape(-1, N_IN), np.tile(idx, free.size)), proto, stats).reshape(free.size, m, -1)
         J = (FJ - F[idx][None]) / steps.T[:, :, None] / tn[idx][None, :, None]   # [5, m, nd]
         J = np.nan_to_num(np.transpose(J, (1, 2, 0)))                # [m, nd, 5]
         r = (F[idx] - T[idx]) / tn[idx][:, None]                     # [m, nd]
@@ -321,7 +332,7 @@ def lm_fit(targets: np.ndarray, start: np.ndarray, proto: Protocol, max_iter: in
         delta = np.clip(delta, -0.5, 0.5)
         un = u[idx].copy()
         un[:, free] = np.clip(un[:, free] + delta, -1.0, 1.0)
-        Fn = sim(from_unit(un, proto), proto, stats)
+        Fn = sim(phys(un, idx), proto, stats)
         en = curve_error(Fn, T[idx])
         en[~np.isfinite(en)] = np.inf
         sims[idx] += free.size + 1
@@ -336,24 +347,64 @@ def lm_fit(targets: np.ndarray, start: np.ndarray, proto: Protocol, max_iter: in
         lam[idx[~better]] = np.minimum(lam[idx[~better]] * 4.0, 1e8)
         rejects[acc] = 0
         rejects[idx[~better]] += 1
-        done = (better & (gain < rtol)) | (rejects[idx] >= 2)
+        done = (better & (gain < rtol)) | (rejects[idx] >= 4)
         active[idx[done]] = False
-    return FitResult(params=from_unit(u, proto), curves=F, error=e, sims=sims, iterations=its,
+    return FitResult(params=phys(u, np.arange(n)), curves=F, error=e, sims=sims, iterations=its,
                      seconds=time.perf_counter() - t0)
 
 
 def surrogate_fit(sur: Surrogate, targets: np.ndarray, indenter_radius: np.ndarray, proto: Protocol,
-                  refine_iter: int = 6, starts: int = 16, stats: SimStats | None = None, simulate=None) -> FitResult:
-    """Surrogate-assisted fit: network proposals (no simulation), one verifying simulation per
-    target, then the simulator's Levenberg-Marquardt from the proposal (stopping as lm_fit does)."""
-    t0 = time.perf_counter()
+                  max_iter: int = 8, starts: int = 16, inner_steps: int = 300, lr: float = 1e-2, rtol: float = 1e-3,
+                  stats: SimStats | None = None, simulate=None) -> FitResult:
+    """Surrogate-assisted fit. Proposals from the network (no simulation); then per iteration one
+    verifying simulation of every active target and a defect-corrected refit of the network's
+    inputs: with d = F_sim(p) - F_net(p) at the current point p, the inputs are refitted (Adam
+    through the network, starting at p) so that F_net matches T - d. A target keeps its best
+    simulated point and stops when an iteration improves its simulated error by less than rtol
+    relative (or makes it worse)."""
     sim = simulate if simulate is not None else simulate_curves
-    P = sur.propose(targets, indenter_radius, starts=starts)
-    F = sim(P, proto, stats)
-    res = lm_fit(targets, P, proto, max_iter=refine_iter, start_curves=F, stats=stats, simulate=sim)
-    res.sims += 1
-    res.seconds = time.perf_counter() - t0
-    return res
+    t0 = time.perf_counter()
+    T = np.asarray(targets, np.float64).reshape(-1, proto.n_depths)
+    n = T.shape[0]
+    p = sur.propose(T, indenter_radius, starts=starts)
+    best_p = p.copy()
+    best_F = np.full_like(T, np.nan)
+    best_e = np.full(n, np.inf)
+    sims = np.zeros(n, np.int64)
+    its = np.zeros(n, np.int64)
+    active = np.ones(n, bool)
+    scale = force_scale(proto)
+    lo_u, hi_u = -np.ones(N_IN, np.float32), np.ones(N_IN, np.float32)
+    for _ in range(max_iter):
+        idx = np.flatnonzero(active)
+        if idx.size == 0:
+            break
+        F = sim(p[idx], proto, stats)
+        sims[idx] += 1
+        its[idx] += 1
+        e = curve_error(F, T[idx])
+        e[~np.isfinite(e)] = np.inf
+        improved = e < best_e[idx] * (1.0 - rtol)
+        better = e < best_e[idx]
+        upd = idx[better]
+        best_p[upd], best_F[upd], best_e[upd] = p[upd], F[better], e[better]
+        active[idx[~improved]] = False
+        go = idx[improved]
+        if go.size == 0:
+            break
+        d = F[improved] - sur.predict(p[go])                 # simulator - network at the current point
+        y = ((T[go] - d) / scale).astype(np.float32)
+        w = (1.0 / np.maximum((T[go] / scale) ** 2, 1e-300).sum(1)).astype(np.float32)
+        u = to_unit(p[go], proto).astype(np.float32)
+        rows = sur.net.max_batch
+        for a in range(0, go.size, rows):
+            u[a:a + rows], _ = sur.net.fit_inputs(u[a:a + rows], y[a:a + rows], FREE_MATERIAL, lo_u, hi_u,
+                                                  steps=inner_steps, lr=lr, weight=w[a:a + rows])
+        q = from_unit(u, proto)
+        q[:, 5] = p[go, 5]  # the known radius stays exact
+        p[go] = q
+    return FitResult(params=best_p, curves=best_F, error=best_e, sims=sims, iterations=its,
+                     seconds=time.perf_counter() - t0)
 
 
 # The full experiment: a radius-16 cell (103,536 tetra), 9,600 steps per curve. The small one

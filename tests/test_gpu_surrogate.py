@@ -1,0 +1,52 @@
+"""The learned part end to end on the small protocol (radius-6 cell, 900 steps per curve): the
+batched simulator generates curves, the MLP kernels train on them, and the surrogate-assisted
+inverse fit reaches the plain simulator-only fit's error with several times fewer full
+simulations. Every error is measured by the simulator, not by the network."""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def experiment():
+    from nofluidx3d_gb300 import surrogate as S
+
+    return S.run_experiment(S.SMALL, n_curves=2048, n_hold=256, n_targets=32, n_plain=32, train_steps=3000,
+                            batch=256, seed=0, log=lambda *a: None)
+
+
+def test_simulated_curves_match_the_plain_path():
+    """simulate_curves (batched, shared mesh) equals CellSim runs of the same inputs."""
+    from nofluidx3d_gb300 import surrogate as S
+    from nofluidx3d_gb300.core import CellSim
+
+    proto = S.SMALL
+    P = S.sample_params(3, proto, seed=11)
+    F = S.simulate_curves(P, proto)
+    mesh = proto.mesh()
+    rows = proto.steps // proto.record_every + 1
+    for i in range(3):
+        s = CellSim(0)
+        S.workload(P[i], proto).configure(s, mesh, max_rows=rows)
+        s.step(proto.steps)
+        s.record_now()
+        c = s.curve()
+        np.testing.assert_array_equal(np.interp(proto.depths(), c[:, 1], c[:, 2]), F[i])
+        s.close()
+    assert np.all(np.isfinite(F)) and np.all(F[:, -1] > 0)
+
+
+def test_surrogate_learns_the_curves(experiment):
+    assert experiment["dataset"]["non_finite"] == 0
+    assert experiment["held_out_curve_error"]["median"] < 0.05
+
+
+def test_surrogate_fit_needs_fewer_simulations(experiment):
+    fit = experiment["inverse_fit"]
+    # same final error as the simulator-only fit (both sit at the 1 % noise floor) ...
+    assert fit["surrogate"]["error"]["median"] <= fit["plain"]["error"]["median"] * 1.05 + 1e-3
+    assert fit["surrogate_error_le_plain_plus_1e-3"] >= 0.9
+    # ... with several times fewer full simulations
+    assert fit["sims_ratio_plain_over_surrogate"] >= 3.0
