@@ -32,6 +32,8 @@ REF_LIB_PATH = HERE / "_ref" / "libnfxref.so"
 
 MODEL_MR, MODEL_SVK, MODEL_SVKK, MODEL_VP = 0, 1, 2, 3
 SUBSTRATE, PLANE, SPHERE = 0, 1, 2
+SPHERE_INTEGRAL = 3  # InteractionSphereIntegral.cl
+INTEGRATOR_VV, INTEGRATOR_VV2 = 0, 1  # VelocityVerlet.cl (unit mass), velocityVerlet2.cl (lumped masses)
 
 
 def build(force: bool = False) -> Path:
@@ -57,7 +59,8 @@ class _Problem(C.Structure):
     _fields_ = [("np", C.c_long), ("nt", C.c_long), ("tets", C.c_void_p), ("edge", C.c_void_p),
                 ("vol", C.c_void_p), ("model", C.c_int), ("E", C.c_double), ("nu", C.c_double),
                 ("mr", C.c_double), ("n_contacts", C.c_int), ("contacts", _Contact * 4),
-                ("xi", C.c_double), ("fix_top_bottom", C.c_int), ("record_contact", C.c_int)]
+                ("xi", C.c_double), ("fix_top_bottom", C.c_int), ("record_contact", C.c_int),
+                ("integrator", C.c_int), ("masses", C.c_void_p)]
 
 
 class _State(C.Structure):
@@ -125,6 +128,8 @@ class Problem:
     xi: float = 0.005
     fix_top_bottom: bool = False
     record_contact: int = -1
+    integrator: int = INTEGRATOR_VV
+    density: float = 1.0  # lumped masses of INTEGRATOR_VV2
 
     @property
     def np_(self) -> int:
@@ -136,6 +141,18 @@ class Problem:
 
     def edge_base(self) -> int:
         return 3 if self.model == MODEL_VP else 0
+
+
+def lumped_masses(points: np.ndarray, tets: np.ndarray, density: float = 1.0) -> np.ndarray:
+    """Nodal masses of VelocityVerlet2, nofluidx3d/SimulationLegacy.py:911-924: every tetra adds a
+    quarter of density * V0 (TetraCell volumes, TetraCell.py:39-41) to each of its corners, in tetra
+    order then corner order, as the reference's Python loop does."""
+    from nofluidx3d_gb300.mesh import signed_volumes  # setup math only
+
+    q = 0.25 * density * signed_volumes(points, tets)
+    m = np.zeros(points.shape[0])
+    np.add.at(m, np.asarray(tets, np.int64).reshape(-1), np.repeat(q, 4))
+    return m
 
 
 class State:
@@ -174,6 +191,8 @@ class State:
         for i, c in enumerate(prob.contacts):
             p.contacts[i] = _Contact(c.kind, c.k, c.radius, c.p0, c.v, min(c.tmove, 1e300))
         p.xi, p.fix_top_bottom, p.record_contact = prob.xi, int(prob.fix_top_bottom), prob.record_contact
+        self.masses = np.ascontiguousarray(lumped_masses(prob.points, prob.tets, prob.density), dtype=dt)
+        p.integrator, p.masses = int(prob.integrator), _ptr(self.masses)
         self._cstate = _State(*[_ptr(a) for a in (self.points, self.vel, self.force, self.fold, self.acc,
                                                   self.Fp, self.vonMises, self.pressure, self.vp_par)])
 
@@ -232,7 +251,10 @@ def ref_lib():
         _ref.ref_plane.argtypes = [v, v, L, d, d]
         _ref.ref_sphere.argtypes = [v, v, L, d, d, d]
         _ref.ref_vv.argtypes = [v, v, v, v, L, d, I]
-        for f in (_ref.ref_tetra, _ref.ref_vp, _ref.ref_substrate, _ref.ref_plane, _ref.ref_sphere, _ref.ref_vv):
+        _ref.ref_vv2.argtypes = [v, v, v, v, v, L, d]
+        _ref.ref_sphere_integral.argtypes = [v, v, v, L, L, d, d, d]
+        for f in (_ref.ref_tetra, _ref.ref_vp, _ref.ref_substrate, _ref.ref_plane, _ref.ref_sphere, _ref.ref_vv,
+                  _ref.ref_vv2, _ref.ref_sphere_integral):
             f.restype = None
     return _ref
 
@@ -268,9 +290,15 @@ def ref_run(st: State, nsteps: int, record_every: int = 0):
                 R.ref_substrate(_ptr(st.force), _ptr(st.points), npn, pos, c.k)
             elif c.kind == PLANE:
                 R.ref_plane(_ptr(st.force), _ptr(st.points), npn, pos, c.k)
+            elif c.kind == SPHERE_INTEGRAL:
+                R.ref_sphere_integral(_ptr(st.force), _ptr(st.points), _ptr(st.tets), npn, nt, c.radius, pos, c.k)
             else:
                 R.ref_sphere(_ptr(st.force), _ptr(st.points), npn, c.radius, pos, c.k)
-        R.ref_vv(_ptr(st.points), _ptr(st.vel), _ptr(st.force), _ptr(st.fold), npn, P.xi, int(P.fix_top_bottom))
+        if P.integrator == INTEGRATOR_VV2:
+            R.ref_vv2(_ptr(st.points), _ptr(st.vel), _ptr(st.force), _ptr(st.fold), _ptr(st.masses), npn, P.xi)
+        else:
+            R.ref_vv(_ptr(st.points), _ptr(st.vel), _ptr(st.force), _ptr(st.fold), npn, P.xi,
+                     int(P.fix_top_bottom))
         st.time += 1
         if record_every > 0 and (s + 1) % record_every == 0:
             record(st.time)

@@ -43,6 +43,8 @@ KERNEL_FILES = [
     "Interactions/Sphere.cl",
     "Interactions/VelocityVerlet.cl",
     "InteractionFiniteStrainViscoplastic.cl",
+    "velocityVerlet2.cl",
+    "InteractionSphereIntegral.cl",
 ]
 
 _VEC_LITERAL = re.compile(r"\((ibmPrecisionFloat3|tetraPrecisionFloat3|double3|float3)\)\s*\(")

@@ -26,10 +26,10 @@
 #endif
 
 enum { ORA_MODEL_MR = 0, ORA_MODEL_SVK = 1, ORA_MODEL_SVKK = 2, ORA_MODEL_VP = 3 };
-enum { ORA_SUBSTRATE = 0, ORA_PLANE = 1, ORA_SPHERE = 2 };
+enum { ORA_SUBSTRATE = 0, ORA_PLANE = 1, ORA_SPHERE = 2, ORA_SPHERE_INTEGRAL = 3 };
 
 typedef struct {
-    int kind;      /* ORA_SUBSTRATE / ORA_PLANE / ORA_SPHERE */
+    int kind;      /* ORA_SUBSTRATE / ORA_PLANE / ORA_SPHERE / ORA_SPHERE_INTEGRAL */
     double k;      /* penalty constant (def_FORCE_CONST) */
     double radius; /* sphere radius */
     double p0;     /* position at t = 0 (wall height or sphere centre height) */
@@ -49,6 +49,8 @@ typedef struct {
     double xi;            /* velocity-Verlet damping */
     int fix_top_bottom;
     int record_contact;   /* contact whose force is recorded, -1 for none */
+    int integrator;       /* 0: VelocityVerlet (unit mass), 1: VelocityVerlet2 (lumped masses) */
+    const void* masses;   /* np real, lumped nodal masses (integrator 1) */
 } ora_problem;
 
 typedef struct {
@@ -87,24 +89,32 @@ static void ora_curve_row(const ora_problem* P, long t, double force, double* ro
 #define SQRT sqrt
 #define POW pow
 #define FMAX fmax
+#define FABS fabs
+#define EXP exp
 #include "oracle_body.h"
 #undef real
 #undef SFX
 #undef SQRT
 #undef POW
 #undef FMAX
+#undef FABS
+#undef EXP
 
 #define real float
 #define SFX _f32
 #define SQRT sqrtf
 #define POW powf
 #define FMAX fmaxf
+#define FABS fabsf
+#define EXP expf
 #include "oracle_body.h"
 #undef real
 #undef SFX
 #undef SQRT
 #undef POW
 #undef FMAX
+#undef FABS
+#undef EXP
 
 /* ------------------------------------------------------------------------------------------ */
 /* OpenMP step (CPU baseline timing). Element work-items run in parallel with atomic adds, the  */
@@ -146,8 +156,13 @@ static void ora_curve_row(const ora_problem* P, long t, double force, double* ro
             vv_node##SFX(i, np, x, (real*)S->vel, f, (real*)S->fold, (real)P->xi, P->fix_top_bottom); \
     }                                                                                               \
     long ora_run_par##SFX(const ora_problem* P, ora_state_p S, long t0, long nsteps, int threads) {  \
+        int serial = P->integrator != 0; /* the parallel step covers the timed workloads only */    \
+        for (int c = 0; c < P->n_contacts; c++) serial |= P->contacts[c].kind == ORA_SPHERE_INTEGRAL; \
         if (threads > 0) omp_set_num_threads(threads);                                              \
-        for (long s = 0; s < nsteps; s++) ora_step_par##SFX(P, S, t0 + s);                          \
+        for (long s = 0; s < nsteps; s++) {                                                         \
+            if (serial) ora_step##SFX(P, S, t0 + s);                                                \
+            else ora_step_par##SFX(P, S, t0 + s);                                                   \
+        }                                                                                           \
         return nsteps;                                                                              \
     }
 

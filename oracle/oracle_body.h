@@ -365,6 +365,71 @@ static inline void NM(vv_node)(long i, long np, real* points, real* vel, real* f
     force[i] = 0; force[np + i] = 0; force[2 * np + i] = 0;
 }
 
+/* Lumped-mass damped velocity Verlet, nofluidx3d/kernels/velocityVerlet2.cl:1-26, dt = 1: the old-force
+ * slot holds the previous acceleration. v <- (v + (a_old + f/m)/2) / (1 + xi/2); a = f/m - xi v;
+ * x <- x + v + a/2; a_old <- a; f <- 0. */
+static inline void NM(vv2_node)(long i, long np, real* points, real* vel, real* force, real* fold,
+                                const real* masses, real xi) {
+    V3 x = NM(load3)(points, np, i), v = NM(load3)(vel, np, i);
+    const V3 f = NM(load3)(force, np, i), ao = NM(load3)(fold, np, i);
+    const real m = masses[i];
+    v = NM(vscale)(NM(vadd)(v, NM(vscale)(NM(vadd)(ao, NM(vdiv)(f, m)), (real)0.5)), (real)1.0 / (1 + xi / (real)2.0));
+    const V3 a = NM(vsub)(NM(vdiv)(f, m), NM(vscale)(v, xi));
+    x = NM(vadd)(NM(vadd)(x, v), NM(vscale)(a, (real)0.5));
+    points[i] = x.x; points[np + i] = x.y; points[2 * np + i] = x.z;
+    vel[i] = v.x; vel[np + i] = v.y; vel[2 * np + i] = v.z;
+    fold[i] = a.x; fold[np + i] = a.y; fold[2 * np + i] = a.z;
+    force[i] = 0; force[np + i] = 0; force[2 * np + i] = 0;
+}
+
+/* Sphere contact integrated over each tetra, nofluidx3d/kernels/InteractionSphereIntegral.cl:22-85:
+ * a repulsive force density exp(-k (|x - c| - R)) (x - c)/|x - c| (c = (0, spos, 0)) evaluated at the
+ * four-point Gauss rule of the tetra (the kernel's truncated coordinates 0.58541020 / 0.13819669)
+ * and distributed to the corners with the linear shape functions, weighted by |det[p1-p4, p2-p4,
+ * p3-p4]| / 4 as the kernel does. */
+static inline V3 NM(si_density)(V3 x, real radius, real spos, real k) {
+    const V3 r = NM(vsub)(x, NM(mk3)(0, spos, 0));
+    const V3 n = NM(vdiv)(r, NM(vlen)(r));
+    const real dis = NM(vlen)(r) - radius;
+    return NM(vscale)(n, EXP(-k * dis));
+}
+static void NM(sphere_integral_tet)(long t, long np, long nt, const real* points, const unsigned* tets, real radius,
+                                    real spos, real k, real* force) {
+    const long ids[4] = {tets[t], tets[nt + t], tets[2 * nt + t], tets[3 * nt + t]};
+    V3 p[4];
+    for (int a = 0; a < 4; a++) p[a] = NM(load3)(points, np, ids[a]);
+    const V3 r1 = NM(vsub)(p[0], p[3]), r2 = NM(vsub)(p[1], p[3]), r3 = NM(vsub)(p[2], p[3]);
+    const real volume = FABS(NM(vdot)(r1, NM(vcross)(r2, r3)));
+    const real al = (real)0.58541020, be = (real)0.13819669;
+    const real xi[4][3] = {{al, be, be}, {be, al, be}, {be, be, al}, {be, be, be}};
+    V3 fg[4];
+    real N[4][4]; /* N[g][a]: shape function a at Gauss point g */
+    for (int g = 0; g < 4; g++) {
+        const real n4 = (real)1.0 - xi[g][0] - xi[g][1] - xi[g][2];
+        const V3 x = NM(vadd)(NM(vadd)(NM(vadd)(NM(vscale)(p[0], xi[g][0]), NM(vscale)(p[1], xi[g][1])),
+                                       NM(vscale)(p[2], xi[g][2])), NM(vscale)(p[3], n4));
+        fg[g] = NM(si_density)(x, radius, spos, k);
+        N[g][0] = xi[g][0]; N[g][1] = xi[g][1]; N[g][2] = xi[g][2]; N[g][3] = n4;
+    }
+    for (int a = 0; a < 4; a++) {
+        V3 s = NM(vadd)(NM(vadd)(NM(vadd)(NM(vscale)(fg[0], N[0][a]), NM(vscale)(fg[1], N[1][a])),
+                                 NM(vscale)(fg[2], N[2][a])), NM(vscale)(fg[3], N[3][a]));
+        NM(add3)(force, np, ids[a], NM(vscale)(s, (real)0.25 * volume));
+    }
+}
+
+/* Readout of the integrated sphere force, nofluidx3d/SimulationLegacy.py:260-273 (lattice units):
+ * the force is recomputed into a zeroed buffer and -sum_i F_y(i) returned (node order, double). */
+double NM(ora_sphere_integral_readout)(long np, long nt, const real* points, const unsigned* tets, real radius,
+                                       real spos, real k) {
+    real* buf = (real*)calloc((size_t)(3 * np), sizeof(real));
+    for (long t = 0; t < nt; t++) NM(sphere_integral_tet)(t, np, nt, points, tets, radius, spos, k, buf);
+    double s = 0;
+    for (long i = 0; i < np; i++) s += (double)buf[np + i];
+    free(buf);
+    return -s;
+}
+
 /* Indenter-force readouts in lattice units (the host closures forceSI without the p0*L0^2 factor).
  * Plane, nofluidx3d/Simulation.py:146-153: sum_i k*max(y_i - wall, 0).
  * Sphere, nofluidx3d/Simulation.py:198-212: -sum_i [k*max(R - |x_i - c|, 0) * (x_i - c)/|x_i - c|]_y.
@@ -405,11 +470,21 @@ void NM(ora_step)(const ora_problem* P, ora_state_p S, long t) {
     for (int c = 0; c < P->n_contacts; c++) {
         const ora_contact* C = &P->contacts[c];
         const real pos = (real)ora_contact_pos(C, (double)t);
+        if (C->kind == ORA_SPHERE_INTEGRAL) {
+            for (long e = 0; e < nt; e++)
+                NM(sphere_integral_tet)(e, np, nt, x, P->tets, (real)C->radius, pos, (real)C->k, f);
+            continue;
+        }
         for (long i = 0; i < np; i++) {
             if (C->kind == ORA_SUBSTRATE) NM(substrate_node)(i, np, x, pos, (real)C->k, f);
             else if (C->kind == ORA_PLANE) NM(plane_node)(i, np, x, pos, (real)C->k, f);
             else NM(sphere_node)(i, np, x, (real)C->radius, pos, (real)C->k, f);
         }
+    }
+    if (P->integrator == 1) {
+        for (long i = 0; i < np; i++)
+            NM(vv2_node)(i, np, x, (real*)S->vel, f, (real*)S->fold, (const real*)P->masses, (real)P->xi);
+        return;
     }
     for (long i = 0; i < np; i++)
         NM(vv_node)(i, np, x, (real*)S->vel, f, (real*)S->fold, (real)P->xi, P->fix_top_bottom);
@@ -421,6 +496,9 @@ double NM(ora_readout)(const ora_problem* P, ora_state_p S, long t) {
     const real pos = (real)ora_contact_pos(C, (double)t);
     if (C->kind == ORA_SPHERE) return NM(ora_sphere_readout)(P->np, (const real*)S->points, (real)C->radius, pos, (real)C->k);
     if (C->kind == ORA_PLANE) return NM(ora_plane_readout)(P->np, (const real*)S->points, pos, (real)C->k);
+    if (C->kind == ORA_SPHERE_INTEGRAL)
+        return NM(ora_sphere_integral_readout)(P->np, P->nt, (const real*)S->points, P->tets, (real)C->radius, pos,
+                                               (real)C->k);
     return 0.0;
 }
 
