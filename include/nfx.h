@@ -44,6 +44,7 @@ extern "C" {
 #define NFX_CONTACT_SUBSTRATE 0 /* nofluidx3d/interactions/Substrate.py, kernels/Interactions/Substrate.cl */
 #define NFX_CONTACT_PLANE 1     /* nofluidx3d/interactions/Plane.py, kernels/Interactions/Plane.cl */
 #define NFX_CONTACT_SPHERE 2    /* nofluidx3d/interactions/Sphere.py, kernels/Interactions/Sphere.cl */
+#define NFX_CONTACT_SPHERE_INTEGRAL 3 /* Interactions.py:601-637, kernels/InteractionSphereIntegral.cl:22-85 */
 
 /* status bits (nfx_status) */
 #define NFX_STATUS_NONFINITE 1u  /* a position/velocity/force became NaN or Inf (util/IO.py:17-28 aborts on this) */
@@ -94,7 +95,10 @@ int nfx_set_viscoplastic(nfx_sim* sim, const double* par8);
  * application after the element force. position(t) = p0 - v*t while t <= tmove, then
  * p0 - v*tmove (the wallFunc/sphereFunc schedules of Simulation.py:117-132, :173-183);
  * substrate: position = p0. k is def_FORCE_CONST (Simulation.py:109, :134, :185).
- * Replaces Substrate(wallPosition, k), Plane(wallFunc, k), Sphere(radius, sphereFunc, k). */
+ * Replaces Substrate(wallPosition, k), Plane(wallFunc, k), Sphere(radius, sphereFunc, k).
+ * NFX_CONTACT_SPHERE_INTEGRAL replaces InteractionSphereIntegral(radius, sphereFunc, forceConst)
+ * (SimulationLegacy.py:206-238): k is its PotentialForceConst (the decay rate of the density),
+ * the force acts per tetra; at most one per simulation. */
 int nfx_add_contact(nfx_sim* sim, int kind, double k, double radius, double p0, double v, double tmove, int* id);
 
 /* Supplies explicit per-step positions pos[0..n) for times t0..t0+n-1 of contact `id`,
@@ -107,6 +111,10 @@ int nfx_set_contact_table(nfx_sim* sim, int id, int64_t t0, int64_t n, const dou
  * FIXED_TOP_BOTTOM pin of user nodes 3 and 4 (VelocityVerlet.cl:17-22,
  * interactions/VelocityVerlet.py:23-45). */
 int nfx_set_integrator(nfx_sim* sim, double xi, int fix_top_bottom);
+/* The lumped-mass velocity Verlet instead (velocityVerlet2.cl:1-26, Interactions.py:818-836): nodal
+ * masses density * sum of V0/4 over the node's tetrahedra (SimulationLegacy.py:911-924, where the
+ * density is 1), damping xi, the old-force slot holding the previous acceleration. */
+int nfx_set_integrator_lumped(nfx_sim* sim, double xi, double density);
 
 /* Records the indenter force of contact `contact` every `every` steps into a device buffer of
  * max_rows rows (t, indentation, force) — the recordedQuantities currentTime / indentationSI /
@@ -199,8 +207,9 @@ int nfx_batch_set_viscoplastic(nfx_batch* batch, int cell, const double* par8);
 /* Per-cell contact (schedule only), as nfx_add_contact. */
 int nfx_batch_add_contact(nfx_batch* batch, int cell, int kind, double k, double radius, double p0, double v,
                           double tmove, int* id);
-/* Per-cell integrator, as nfx_set_integrator. */
+/* Per-cell integrator, as nfx_set_integrator / nfx_set_integrator_lumped. */
 int nfx_batch_set_integrator(nfx_batch* batch, int cell, double xi, int fix_top_bottom);
+int nfx_batch_set_integrator_lumped(nfx_batch* batch, int cell, double xi, double density);
 /* Records contact index `contact` of every cell every `every` steps into max_rows rows per cell. */
 int nfx_batch_set_record(nfx_batch* batch, int contact, int64_t every, int64_t max_rows);
 /* Builds the cells' plans on host threads (after autotuning the tile size when requested),
@@ -264,6 +273,9 @@ typedef struct nfx_mlp nfx_mlp;
 int nfx_mlp_create(int device, int n_in, int width, int depth, int n_out, int64_t max_batch, nfx_mlp** out);
 int nfx_mlp_destroy(nfx_mlp* mlp);
 int nfx_mlp_num_params(nfx_mlp* mlp, int64_t* n);
+/* Output gain: y = exp(alpha * x[input]) * (last layer's output); input -1 removes it. The
+ * gradients (parameters and inputs) are those of y. */
+int nfx_mlp_set_output_gain(nfx_mlp* mlp, int input, float alpha);
 /* Sets the FP32 master parameters (and their BF16 copies); resets the AdamW moments and step. */
 int nfx_mlp_set_params(nfx_mlp* mlp, const float* params);
 int nfx_mlp_get_params(nfx_mlp* mlp, float* params);

@@ -18,7 +18,8 @@ import time
 import numpy as np
 
 from .core import CellSim
-from .interactions import FiniteStrainViscoplastic, Plane, Sphere, Substrate, Tetra, VelocityVerlet
+from .interactions import (FiniteStrainViscoplastic, Plane, Sphere, SphereIntegral, Substrate, Tetra, VelocityVerlet,
+                           VelocityVerlet2)
 from .TetraCell import TetraCell
 from .util.Bridge import Bridge
 from .util.IO import writeVTK
@@ -153,6 +154,33 @@ class Simulation:
             self.recordedQuantities.append(forceSI)
         return sphere
 
+    def setInteractionSphereIntegral(self, record=True, isSpherical=True):
+        """Sphere contact integrated over the tetrahedra, as SimulationLegacy.py:206-273: the decay
+        rate is the configuration's PotentialForceConst; the recorded force is -sum of the y
+        forces times p0 L0^2 ReynoldScaling YoungsScaling."""
+        radius = self.parameters["SphereRadiusSI"] / self.L0
+        if isSpherical:
+            start = self.parameters["CELL"]["RadiusSIM"] + radius + self.parameters["InitialDistance"]
+        else:
+            start = self.cell.mesh.points[3][1] + radius + self.parameters["InitialDistance"]
+        v, tmove = self._move_params()
+        sphereFunc = _linear_schedule(start, v, tmove)
+        sphere = SphereIntegral(radius, sphereFunc, self.parameters["PotentialForceConst"])
+        self.register(sphere)
+
+        def indentationSI():
+            return (sphereFunc(0) - sphereFunc(self.time)) * self.L0
+
+        def forceSI():
+            scale = (self.p0 * self.L0**2 * self.parameters.get("ReynoldScaling", 1.0)
+                     * self.parameters["CELL"].get("YoungsScaling", 1.0))
+            return self.handle.indenter_force(sphere.contactId) * scale
+
+        if record:
+            self.recordedQuantities.append(indentationSI)
+            self.recordedQuantities.append(forceSI)
+        return sphere
+
     def setInteractionTetra(self):
         youngsModulusSI = self.parameters["CELL"]["YoungsModulusSI"]
         poissonRatio = self.parameters["CELL"]["PoissonRatio"]
@@ -180,6 +208,10 @@ class Simulation:
     # Velocity Verlet last, as in the reference (Simulation.py:227)
     def setInteractionVelocityVerlet(self, fixTopBottom=False, damping=0.005):
         self.register(VelocityVerlet(self.numPoints, fixTopBottom, damping))
+
+    # the lumped-mass form, SimulationLegacy.py:911-924 (density 1)
+    def setInteractionVelocityVerlet2(self, damping=0.1):
+        self.register(VelocityVerlet2(self.numPoints, damping))
 
     def _advance(self, n: int):
         for interaction in self.interactions:

@@ -17,7 +17,7 @@ NFX_OK = 0
 ERR_NAMES = {1: "NFX_ERR_ARG", 2: "NFX_ERR_CUDA", 3: "NFX_ERR_STATE", 4: "NFX_ERR_NOMEM", 5: "NFX_ERR_NODEVICE"}
 
 MODEL_MR, MODEL_SVK, MODEL_SVKK, MODEL_VP = 0, 1, 2, 3
-CONTACT_SUBSTRATE, CONTACT_PLANE, CONTACT_SPHERE = 0, 1, 2
+CONTACT_SUBSTRATE, CONTACT_PLANE, CONTACT_SPHERE, CONTACT_SPHERE_INTEGRAL = 0, 1, 2, 3
 STATUS_NONFINITE, STATUS_INVERTED, STATUS_CURVE_FULL = 1, 2, 4
 FIELD_VON_MISES, FIELD_PRESSURE, FIELD_PLASTIC_STRAIN = 0, 1, 2
 
@@ -47,6 +47,7 @@ _SIGS = {
                          C.POINTER(C.c_int)], C.c_int),
     "nfx_set_contact_table": ([_vp, C.c_int, _i64, _i64, _vp], C.c_int),
     "nfx_set_integrator": ([_vp, C.c_double, C.c_int], C.c_int),
+    "nfx_set_integrator_lumped": ([_vp, C.c_double, C.c_double], C.c_int),
     "nfx_set_record": ([_vp, C.c_int, _i64, _i64], C.c_int),
     "nfx_step": ([_vp, _i64], C.c_int),
     "nfx_record_now": ([_vp], C.c_int),
@@ -77,6 +78,7 @@ _SIGS = {
     "nfx_batch_add_contact": ([_vp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                C.POINTER(C.c_int)], C.c_int),
     "nfx_batch_set_integrator": ([_vp, C.c_int, C.c_double, C.c_int], C.c_int),
+    "nfx_batch_set_integrator_lumped": ([_vp, C.c_int, C.c_double, C.c_double], C.c_int),
     "nfx_batch_set_record": ([_vp, C.c_int, _i64, _i64], C.c_int),
     "nfx_batch_finalize": ([_vp], C.c_int),
     "nfx_batch_step": ([_vp, _i64], C.c_int),
@@ -91,6 +93,7 @@ _SIGS = {
     "nfx_mlp_create": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _i64, C.POINTER(_vp)], C.c_int),
     "nfx_mlp_destroy": ([_vp], C.c_int),
     "nfx_mlp_num_params": ([_vp, C.POINTER(_i64)], C.c_int),
+    "nfx_mlp_set_output_gain": ([_vp, C.c_int, C.c_float], C.c_int),
     "nfx_mlp_set_params": ([_vp, _vp], C.c_int),
     "nfx_mlp_get_params": ([_vp, _vp], C.c_int),
     "nfx_mlp_get_grads": ([_vp, _vp], C.c_int),

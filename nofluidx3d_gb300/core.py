@@ -108,6 +108,10 @@ class CellSim:
     def set_integrator(self, xi: float, fix_top_bottom: bool = False) -> None:
         check(self._L.nfx_set_integrator(self._h, float(xi), int(bool(fix_top_bottom))))
 
+    def set_integrator_lumped(self, xi: float, density: float = 1.0) -> None:
+        """Lumped-mass velocity Verlet (velocityVerlet2.cl)."""
+        check(self._L.nfx_set_integrator_lumped(self._h, float(xi), float(density)))
+
     def set_record(self, contact: int, every: int, max_rows: int) -> None:
         check(self._L.nfx_set_record(self._h, int(contact), int(every), int(max_rows)))
 
@@ -259,6 +263,9 @@ class Batch:
 
     def set_integrator(self, cell: int, xi: float, fix_top_bottom: bool = False) -> None:
         check(self._L.nfx_batch_set_integrator(self._h, int(cell), float(xi), int(bool(fix_top_bottom))))
+
+    def set_integrator_lumped(self, cell: int, xi: float, density: float = 1.0) -> None:
+        check(self._L.nfx_batch_set_integrator_lumped(self._h, int(cell), float(xi), float(density)))
 
     def set_record(self, contact: int, every: int, max_rows: int) -> None:
         check(self._L.nfx_batch_set_record(self._h, int(contact), int(every), int(max_rows)))

@@ -165,9 +165,22 @@ cudaError_t launch_nodes(nfx_sim* s, int k, int mode, int readout_contact) {
     return launch_node_pass(s->mesh, s->st, table_view(s), s->nblocks, k, mode, readout_contact, s->stream);
 }
 
+// The integrated sphere contact's own tile pass, when the cell has one.
+cudaError_t launch_si(nfx_sim* s, int k) {
+    if (s->cell.si_contact < 0) return cudaSuccess;
+    return launch_si_pass(s->mesh, s->st, table_view(s), k, false, -1, s->stream);
+}
+
+// Before a readout of contact `contact` between steps: the integrated sphere's tile partials.
+cudaError_t prepare_readout(nfx_sim* s, int contact) {
+    if (contact < 0 || contact != s->cell.si_contact) return cudaSuccess;
+    return launch_si_pass(s->mesh, s->st, table_view(s), 0, true, contact, s->stream);
+}
+
 int enqueue_steps(nfx_sim* s, int n) {
     for (int k = 0; k < n; k++) {
         CUDA_TRY(launch_elem(s, k));
+        CUDA_TRY(launch_si(s, k));
         CUDA_TRY(launch_nodes(s, k, NODE_UPDATE, -1));
     }
     CUDA_TRY(launch_advance_time(s->st, n, s->fields_every, s->record_every, s->stream));
@@ -251,6 +264,8 @@ int nfx_create(int device, nfx_sim** out) {
     s->st.force_out = s->d_force_out;
     s->cell.record_contact = -1;
     s->cell.fix_a = s->cell.fix_b = -1;
+    s->cell.si_contact = -1;
+    s->cell.integrator = INTEGRATOR_VV;
     cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, device);
     if (s->sm_count < 1) s->sm_count = 1;
     if (const char* v = std::getenv("NFX_TET_KERNEL")) s->tet_variant = std::atoi(v) == 1 ? 1 : 0;
@@ -303,7 +318,7 @@ int nfx_set_mesh(nfx_sim* s, int64_t np, int64_t nt, const double* points, const
     const MeshPlan& P = s->plan;
     auto& A = s->mesh_allocs;
     int* tb; int* nbg; unsigned* tm; uint2* tn; uchar4* lc; ushort4* ti; float4 *da, *db; float2* dc;
-    float4 *xh, *xl, *uh, *ul, *v, *fo; unsigned long long* fa; double* part;
+    float4 *xh, *xl, *uh, *ul, *v, *fo; unsigned long long* fa; double* part; double* tpart;
     const int64_t ns = P.nslots;
     const size_t ntp = (size_t)ns + ARRAY_PAD;  // per-slot arrays carry ARRAY_PAD zeroed elements
     if ((rc = dalloc(s, &tb, P.tile_tet_begin.size(), &A)) || (rc = dalloc(s, &nbg, P.tile_node_begin.size(), &A)) ||
@@ -314,6 +329,7 @@ int nfx_set_mesh(nfx_sim* s, int64_t np, int64_t nt, const double* points, const
         (rc = dalloc(s, &xh, (size_t)np, &A)) || (rc = dalloc(s, &xl, (size_t)np, &A)) || (rc = dalloc(s, &uh, (size_t)np, &A)) ||
         (rc = dalloc(s, &ul, (size_t)np, &A)) || (rc = dalloc(s, &v, (size_t)np, &A)) || (rc = dalloc(s, &fo, (size_t)np, &A)) ||
         (rc = dalloc(s, &fa, 3 * (size_t)np, &A)) || (rc = dalloc(s, &part, (size_t)((np + NODE_BLOCK - 1) / NODE_BLOCK), &A)) ||
+        (rc = dalloc(s, &tpart, (size_t)P.ntiles, &A)) ||
         (rc = dalloc(s, &s->d_node_user, (size_t)np, &A)) || (rc = dalloc(s, &s->d_stage, 9 * (size_t)std::max(np, ns), &A))) {
         free_mesh(s);
         return rc;
@@ -375,6 +391,7 @@ int nfx_set_mesh(nfx_sim* s, int64_t np, int64_t nt, const double* points, const
     s->st.fo = fo;
     s->st.facc = fa;
     s->st.partials = part;
+    s->st.tile_partials = tpart;
     s->time = 0;
     s->rows_written = 0;
     s->nblocks = (int)((np + NODE_BLOCK - 1) / NODE_BLOCK);
@@ -383,6 +400,8 @@ int nfx_set_mesh(nfx_sim* s, int64_t np, int64_t nt, const double* points, const
     s->cell.node_end = (int)np;
     s->cell.block_begin = 0;
     s->cell.block_end = s->nblocks;
+    s->cell.tile_begin = 0;
+    s->cell.tile_end = (int)P.ntiles;
     s->cell_dirty = true;
     s->have_mesh = true;
     // the viscoplastic state follows the mesh
@@ -445,10 +464,14 @@ int nfx_set_viscoplastic(nfx_sim* s, const double* par) {
 
 int nfx_add_contact(nfx_sim* s, int kind, double k, double radius, double p0, double v, double tmove, int* id) {
     CHECK_ARG(s, "null handle");
-    CHECK_ARG(kind == NFX_CONTACT_SUBSTRATE || kind == NFX_CONTACT_PLANE || kind == NFX_CONTACT_SPHERE, "unknown contact kind");
+    CHECK_ARG(kind == NFX_CONTACT_SUBSTRATE || kind == NFX_CONTACT_PLANE || kind == NFX_CONTACT_SPHERE ||
+                  kind == NFX_CONTACT_SPHERE_INTEGRAL,
+              "unknown contact kind");
     CHECK_ARG(s->cell.n_contacts < MAX_CONTACTS, "at most 4 contacts");
+    CHECK_ARG(kind != NFX_CONTACT_SPHERE_INTEGRAL || s->cell.si_contact < 0, "at most one integrated sphere contact");
     CHECK_ARG(std::isfinite(k) && std::isfinite(p0) && std::isfinite(v) && !std::isnan(tmove), "non-finite contact parameter");
-    CHECK_ARG(kind != NFX_CONTACT_SPHERE || radius > 0, "sphere radius must be positive");
+    CHECK_ARG((kind != NFX_CONTACT_SPHERE && kind != NFX_CONTACT_SPHERE_INTEGRAL) || radius > 0,
+              "sphere radius must be positive");
     int rc;
     if ((rc = set_device(s)) != NFX_OK) return rc;
     const int i = s->cell.n_contacts;
@@ -465,6 +488,10 @@ int nfx_add_contact(nfx_sim* s, int kind, double k, double radius, double p0, do
     c.meta = s->d_meta[i];
     s->cell.c[i] = c;
     s->cell.n_contacts++;
+    if (kind == NFX_CONTACT_SPHERE_INTEGRAL) {
+        s->cell.si_contact = i;
+        invalidate_graph(s);  // the step gains the integrated sphere's pass
+    }
     s->cell_dirty = true;
     if (id) *id = i;
     return NFX_OK;
@@ -502,6 +529,7 @@ int nfx_set_integrator(nfx_sim* s, double xi, int fix_top_bottom) {
     CHECK_ARG(std::isfinite(xi) && xi > -2.0, "bad damping");
     // v' = (v (1 - xi/2) + (f + fo)/2) / (1 + xi/2);  x' = x + v'(1 - xi/2) + f/2  (VelocityVerlet.cl:12-14)
     if (fix_top_bottom && !s->have_mesh) return fail(NFX_ERR_STATE, "set the mesh before pinning nodes 3 and 4");
+    s->cell.integrator = INTEGRATOR_VV;
     s->cell.vv_a = (float)((1 - 0.5 * xi) / (1 + 0.5 * xi));
     s->cell.vv_hb = (float)(0.5 / (1 + 0.5 * xi));
     s->cell.vv_dm = (float)(1 - 0.5 * xi);
@@ -510,6 +538,20 @@ int nfx_set_integrator(nfx_sim* s, double xi, int fix_top_bottom) {
         if (s->plan.np > 3) s->cell.fix_a = (int)s->plan.node_int[3];
         if (s->plan.np > 4) s->cell.fix_b = (int)s->plan.node_int[4];
     }
+    s->cell_dirty = true;
+    return NFX_OK;
+}
+
+int nfx_set_integrator_lumped(nfx_sim* s, double xi, double density) {
+    CHECK_ARG(s, "null handle");
+    CHECK_ARG(std::isfinite(xi) && xi > -2.0, "bad damping");
+    CHECK_ARG(std::isfinite(density) && density > 0, "density must be positive");
+    // velocityVerlet2.cl:9-13 with the lumped masses of SimulationLegacy.py:911-924
+    s->cell.integrator = INTEGRATOR_VV2;
+    s->cell.vv2_c = (float)(1.0 / (1.0 + 0.5 * xi));
+    s->cell.vv2_xi = (float)xi;
+    s->cell.inv_density = (float)(1.0 / density);
+    s->cell.fix_a = s->cell.fix_b = -1;
     s->cell_dirty = true;
     return NFX_OK;
 }
@@ -565,6 +607,7 @@ int nfx_record_now(nfx_sim* s) {
     if ((rc = set_device(s)) != NFX_OK) return rc;
     if (s->cell.record_contact < 0) return NFX_OK;
     if ((rc = upload_cell(s)) != NFX_OK) return rc;
+    CUDA_TRY(prepare_readout(s, s->cell.record_contact));
     CUDA_TRY(launch_nodes(s, 0, NODE_READOUT_ROW, -1));
     note_rows(s, s->time, s->time);
     return NFX_OK;
@@ -703,6 +746,7 @@ int nfx_indenter_force(nfx_sim* s, int contact, double* out) {
     CHECK_ARG(contact >= 0 && contact < s->cell.n_contacts, "contact id out of range");
     if ((rc = set_device(s)) != NFX_OK) return rc;
     if ((rc = upload_cell(s)) != NFX_OK) return rc;
+    CUDA_TRY(prepare_readout(s, contact));
     CUDA_TRY(launch_nodes(s, 0, NODE_READOUT_VALUE, contact));
     CUDA_TRY(cudaMemcpyAsync(out, s->d_force_out, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     CUDA_TRY(cudaStreamSynchronize(s->stream));
@@ -758,6 +802,7 @@ int nfx_profile_steps(nfx_sim* s, int64_t nsteps, float* tet_ms, float* node_ms)
     for (int64_t k = 0; k < nsteps && err == cudaSuccess; k++) {
         cudaEventRecord(ev[3 * k], s->stream);
         err = launch_elem(s, 0);
+        if (err == cudaSuccess) err = launch_si(s, 0);
         cudaEventRecord(ev[3 * k + 1], s->stream);
         if (err == cudaSuccess) err = launch_nodes(s, 0, NODE_UPDATE, -1);
         cudaEventRecord(ev[3 * k + 2], s->stream);

@@ -54,6 +54,9 @@ struct CellHost {
     ContactDev c[MAX_CONTACTS]{};
     double xi = 0.005;
     bool fix_top_bottom = false;
+    int integrator = INTEGRATOR_VV;
+    double density = 1.0;
+    int si_contact = -1;
     std::shared_ptr<MeshPlan> plan;  // shared by every cell with the same mesh
     // placement in the concatenated arrays
     int64_t node_base = 0, tet_base = 0, tile_base = 0, block_base = 0, nblocks = 0;
@@ -94,6 +97,7 @@ struct nfx_batch {
     std::vector<int> tuned;    // tile sizes the autotuner tried
     std::vector<float> tuned_ms;
     long long* d_zero_meta = nullptr;
+    bool has_si = false;  // some cell has an integrated sphere contact
 };
 
 namespace {
@@ -213,8 +217,15 @@ int build_device(nfx_batch* b, const std::vector<int>& which, int tile_tets, Bat
         C.vv_a = (float)((1 - 0.5 * xi) / (1 + 0.5 * xi));
         C.vv_hb = (float)(0.5 / (1 + 0.5 * xi));
         C.vv_dm = (float)(1 - 0.5 * xi);
+        C.integrator = c.integrator;
+        C.vv2_c = (float)(1.0 / (1.0 + 0.5 * xi));
+        C.vv2_xi = (float)xi;
+        C.inv_density = (float)(1.0 / c.density);
+        C.si_contact = c.si_contact;
+        C.tile_begin = (int)c.tile_base;
+        C.tile_end = (int)(c.tile_base + P.ntiles);
         C.fix_a = C.fix_b = -1;
-        if (c.fix_top_bottom) {
+        if (c.fix_top_bottom && c.integrator == INTEGRATOR_VV) {
             if (c.np > 3) C.fix_a = (int)(c.node_base + P.node_int[3]);
             if (c.np > 4) C.fix_b = (int)(c.node_base + P.node_int[4]);
         }
@@ -230,6 +241,7 @@ int build_device(nfx_batch* b, const std::vector<int>& which, int tile_tets, Bat
     auto& A = D.allocs;
     int* d_ttb; int* d_tnb; unsigned* d_tm; uint2* d_tn; uchar4* d_lc; ushort4* d_ti; float4 *d_da, *d_db; float2* d_dc;
     float4 *d_xh, *d_xl, *d_uh, *d_ul, *d_v, *d_fo; unsigned long long* d_fa; double* d_part; double* d_fout;
+    double* d_tpart;
     CellDev* d_cells; int *d_tc, *d_bc; unsigned* d_cc; double* d_curves = nullptr;
     float4 *d_pa = nullptr, *d_pb = nullptr; float2 *d_pc = nullptr, *d_fields = nullptr;
     int rc;
@@ -240,6 +252,7 @@ int build_device(nfx_batch* b, const std::vector<int>& which, int tile_tets, Bat
         (rc = balloc(A, &d_xh, np)) || (rc = balloc(A, &d_xl, np)) || (rc = balloc(A, &d_uh, np)) ||
         (rc = balloc(A, &d_ul, np)) || (rc = balloc(A, &d_v, np)) || (rc = balloc(A, &d_fo, np)) ||
         (rc = balloc(A, &d_fa, 3 * (size_t)np)) || (rc = balloc(A, &d_part, nblocks)) || (rc = balloc(A, &d_fout, cells.size())) ||
+        (rc = balloc(A, &d_tpart, ntiles)) ||
         (rc = balloc(A, &d_cells, cells.size())) || (rc = balloc(A, &d_tc, ntiles)) || (rc = balloc(A, &d_bc, nblocks)) ||
         (rc = balloc(A, &d_cc, cells.size())) || (rc = balloc(A, &d_curves, 3 * rows * cells.size())) ||
         (rc = balloc(A, &D.d_clock, 1)) || (rc = balloc(A, &D.d_status, 1)))
@@ -308,6 +321,7 @@ int build_device(nfx_batch* b, const std::vector<int>& which, int tile_tets, Bat
     S.status = D.d_status;
     S.clock = D.d_clock;
     S.partials = d_part;
+    S.tile_partials = d_tpart;
     S.force_out = d_fout;
     BatchDev& B = D.bd;
     B.cells = d_cells;
@@ -327,6 +341,7 @@ int build_device(nfx_batch* b, const std::vector<int>& which, int tile_tets, Bat
 int enqueue_batch_steps(nfx_batch* b, BatchDevice& D, int n) {
     for (int k = 0; k < n; k++) {
         BCUDA(launch_tet_pass(D.mesh, D.st, D.bd, b->model, k, b->stream));
+        if (b->has_si) BCUDA(launch_si_pass(D.mesh, D.st, D.bd, k, false, -1, b->stream));
         BCUDA(launch_node_pass(D.mesh, D.st, D.bd, D.nblocks, k, NODE_UPDATE, -1, b->stream));
     }
     BCUDA(launch_advance_time(D.st, n, D.bd.fields_every, D.bd.record_every, b->stream));
@@ -548,9 +563,13 @@ int nfx_batch_add_contact(nfx_batch* b, int cell, int kind, double k, double rad
     if (b->finalized) return bfail(NFX_ERR_STATE, "batch already finalized");
     CellHost& c = b->cells[cell];
     BARG(c.n_contacts < MAX_CONTACTS, "at most 4 contacts per cell");
-    BARG(kind == NFX_CONTACT_SUBSTRATE || kind == NFX_CONTACT_PLANE || kind == NFX_CONTACT_SPHERE, "unknown contact kind");
+    BARG(kind == NFX_CONTACT_SUBSTRATE || kind == NFX_CONTACT_PLANE || kind == NFX_CONTACT_SPHERE ||
+             kind == NFX_CONTACT_SPHERE_INTEGRAL,
+         "unknown contact kind");
     BARG(std::isfinite(k) && std::isfinite(p0) && std::isfinite(v) && !std::isnan(tmove), "non-finite contact parameter");
-    BARG(kind != NFX_CONTACT_SPHERE || radius > 0, "sphere radius must be positive");
+    BARG((kind != NFX_CONTACT_SPHERE && kind != NFX_CONTACT_SPHERE_INTEGRAL) || radius > 0,
+         "sphere radius must be positive");
+    BARG(kind != NFX_CONTACT_SPHERE_INTEGRAL || c.si_contact < 0, "at most one integrated sphere contact per cell");
     ContactDev& C = c.c[c.n_contacts];
     C = ContactDev{};
     C.kind = kind;
@@ -560,6 +579,10 @@ int nfx_batch_add_contact(nfx_batch* b, int cell, int kind, double k, double rad
     C.v = v;
     C.tmove = tmove;
     if (id) *id = c.n_contacts;
+    if (kind == NFX_CONTACT_SPHERE_INTEGRAL) {
+        c.si_contact = c.n_contacts;
+        b->has_si = true;
+    }
     c.n_contacts++;
     return NFX_OK;
 }
@@ -571,6 +594,21 @@ int nfx_batch_set_integrator(nfx_batch* b, int cell, double xi, int fix_top_bott
     BARG(std::isfinite(xi) && xi > -2.0, "bad damping");
     b->cells[cell].xi = xi;
     b->cells[cell].fix_top_bottom = fix_top_bottom != 0;
+    b->cells[cell].integrator = INTEGRATOR_VV;
+    return NFX_OK;
+}
+
+int nfx_batch_set_integrator_lumped(nfx_batch* b, int cell, double xi, double density) {
+    int rc;
+    if ((rc = check_cell(b, cell)) != NFX_OK) return rc;
+    if (b->finalized) return bfail(NFX_ERR_STATE, "batch already finalized");
+    BARG(std::isfinite(xi) && xi > -2.0, "bad damping");
+    BARG(std::isfinite(density) && density > 0, "density must be positive");
+    CellHost& c = b->cells[cell];
+    c.xi = xi;
+    c.fix_top_bottom = false;
+    c.integrator = INTEGRATOR_VV2;
+    c.density = density;
     return NFX_OK;
 }
 
@@ -659,6 +697,8 @@ int nfx_batch_record_now(nfx_batch* b) {
     BARG(b, "null batch");
     if (!b->finalized) return bfail(NFX_ERR_STATE, "call nfx_batch_finalize first");
     BCUDA(cudaSetDevice(b->device));
+    if (b->has_si && b->record_contact >= 0)
+        BCUDA(launch_si_pass(b->dev.mesh, b->dev.st, b->dev.bd, 0, true, b->record_contact, b->stream));
     BCUDA(launch_node_pass(b->dev.mesh, b->dev.st, b->dev.bd, b->dev.nblocks, 0, NODE_READOUT_ROW, -1, b->stream));
     note_batch_rows(b, b->time, b->time);
     return NFX_OK;
@@ -669,6 +709,7 @@ int nfx_batch_indenter_force(nfx_batch* b, int contact, double* out) {
     BARG(contact >= 0 && contact < MAX_CONTACTS, "contact id out of range");
     if (!b->finalized) return bfail(NFX_ERR_STATE, "call nfx_batch_finalize first");
     BCUDA(cudaSetDevice(b->device));
+    if (b->has_si) BCUDA(launch_si_pass(b->dev.mesh, b->dev.st, b->dev.bd, 0, true, contact, b->stream));
     BCUDA(launch_node_pass(b->dev.mesh, b->dev.st, b->dev.bd, b->dev.nblocks, 0, NODE_READOUT_VALUE, contact, b->stream));
     BCUDA(cudaMemcpyAsync(out, b->dev.st.force_out, b->cells.size() * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
     BCUDA(cudaStreamSynchronize(b->stream));

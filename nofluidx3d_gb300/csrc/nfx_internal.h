@@ -10,7 +10,8 @@
 namespace nfx {
 
 enum Model : int { MODEL_MR = 0, MODEL_SVK = 1, MODEL_SVKK = 2, MODEL_VP = 3 };
-enum ContactKind : int { CONTACT_SUBSTRATE = 0, CONTACT_PLANE = 1, CONTACT_SPHERE = 2 };
+enum ContactKind : int { CONTACT_SUBSTRATE = 0, CONTACT_PLANE = 1, CONTACT_SPHERE = 2, CONTACT_SPHERE_INTEGRAL = 3 };
+enum Integrator : int { INTEGRATOR_VV = 0, INTEGRATOR_VV2 = 1 };
 
 constexpr int MAX_CONTACTS = 4;
 // A tile is a run of consecutive tetrahedra (after reordering) processed by one CTA. Its
@@ -60,7 +61,8 @@ struct MeshPlan {
     std::vector<uint16_t> tile_inc;        // 4 * nslots: per tile, the corners (4*local tet + corner)
                                            // grouped by local node in node order, tet order within
     std::vector<float> dmi;                // 12 * nslots: Dm^-1 row-major (9), V0, pad, pad
-    std::vector<float> Xh, Xl;             // 4 * np: reference position hi / lo parts
+    std::vector<float> Xh, Xl;             // 4 * np: reference position hi / lo parts; Xh.w holds the
+                                           // inverse lumped mass of density 1 (VelocityVerlet2)
 };
 
 // Builds the plan from the reference's layouts (points SoA 3*np doubles, tets SoA 4*nt).
@@ -83,7 +85,7 @@ struct MeshDev {
     const float4* dmi_a;  // Dm^-1 entries 0..3
     const float4* dmi_b;  // Dm^-1 entries 4..7
     const float2* dmi_c;  // Dm^-1 entry 8, V0
-    const float4* Xh;
+    const float4* Xh;  // w: inverse lumped mass at density 1
     const float4* Xl;
 };
 
@@ -115,6 +117,7 @@ struct StateDev {
     unsigned* status;
     StepClock* clock;    // time at the start of the current chunk + schedule masks
     double* partials;    // one per node block, for the deterministic readout reduction
+    double* tile_partials;  // one per tile: the tile's share of an integrated-sphere readout
     double* force_out;   // per cell: result of an on-demand readout
 };
 
@@ -154,6 +157,10 @@ struct CellDev {
     int record_contact;           // -1: none
     int node_begin, node_end;     // the cell's nodes in the global arrays
     int block_begin, block_end;   // the cell's node blocks
+    int tile_begin, tile_end;     // the cell's tiles
+    int integrator;               // INTEGRATOR_VV (unit mass) or INTEGRATOR_VV2 (lumped masses)
+    float vv2_c, vv2_xi, inv_density;  // VelocityVerlet2: 1 / (1 + xi/2), xi, 1 / density
+    int si_contact;               // index of the integrated sphere contact, -1: none
 };
 
 struct BatchDev {
@@ -187,6 +194,12 @@ cudaError_t launch_node_pass(const MeshDev& m, const StateDev& s, const BatchDev
 // Advance the clock by n steps (n = 0: refresh the masks only) for the given schedules.
 cudaError_t launch_advance_time(const StateDev& s, long long n, long long fields_every, long long record_every,
                                 cudaStream_t stream);
+// Integrated sphere contact over all tiles (tiles of cells without one return at once). Inside a
+// step (readout false): its forces join the accumulator and, on record steps, the tile partials
+// of the readout are written. readout true: only the tile partials of contact index `contact` at
+// the current positions, for readouts between steps.
+cudaError_t launch_si_pass(const MeshDev& m, const StateDev& s, const BatchDev& b, int t_offset, bool readout,
+                           int contact, cudaStream_t stream);
 // Conversions between the user's layout (SoA doubles, user order) and the device state.
 cudaError_t launch_points_to_user(const MeshDev& m, const StateDev& s, const long long* node_user, double* out,
                                   cudaStream_t stream);

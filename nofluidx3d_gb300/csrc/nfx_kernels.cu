@@ -126,6 +126,99 @@ __device__ __forceinline__ void node_flush(uint2 node, const unsigned short* inc
 
 __device__ __forceinline__ bool clock_bit(const unsigned* mask, int k) { return (mask[k >> 5] >> (k & 31)) & 1u; }
 
+// Sphere centre height, radius and decay rate of an integrated sphere contact for one step.
+struct SphereIntegralStep {
+    float cy_hi, cy_lo, radius, k;
+};
+
+// Integrated sphere contact of one tetra (InteractionSphereIntegral.cl:22-85): the repulsive
+// density exp(-k (|x - c| - R)) (x - c)/|x - c| at the four-point Gauss rule (the kernel's
+// coordinates 0.58541020 / 0.13819669), distributed with the linear shape functions and weighted
+// by |det[p1-p4, p2-p4, p3-p4]| / 4 (the current, deformed tetra). Corner positions relative to
+// the centre and the edges are formed from the hi/lo parts of X and u, so large coordinates lose
+// no precision. Adds the corner forces to the tetra's slots when s_cf is given; returns the sum
+// of their y components (the readout's share).
+template <int TILE>
+__device__ __forceinline__ float sphere_integral(int j, uchar4 lc, const float4* s_uh, const float4* s_ul,
+                                                 const float4* s_xh, const float4* s_xl, const SphereIntegralStep& sp,
+                                                 float4* s_cf) {
+    const int li[4] = {lc.x, lc.y, lc.z, lc.w};
+    float4 xh[4], xl[4], uh[4], ul[4];
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        xh[a] = s_xh[li[a]];
+        xl[a] = s_xl[li[a]];
+        uh[a] = s_uh[li[a]];
+        ul[a] = s_ul[li[a]];
+    }
+    float d[4][3];  // corner minus sphere centre (0, cy, 0)
+    float e[3][3];  // corners 1..3 minus corner 4
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        d[a][0] = (xh[a].x + uh[a].x) + (xl[a].x + ul[a].x);
+        d[a][1] = ((xh[a].y - sp.cy_hi) + uh[a].y) + ((xl[a].y - sp.cy_lo) + ul[a].y);
+        d[a][2] = (xh[a].z + uh[a].z) + (xl[a].z + ul[a].z);
+    }
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        e[a][0] = ((xh[a].x - xh[3].x) + (uh[a].x - uh[3].x)) + ((xl[a].x - xl[3].x) + (ul[a].x - ul[3].x));
+        e[a][1] = ((xh[a].y - xh[3].y) + (uh[a].y - uh[3].y)) + ((xl[a].y - xl[3].y) + (ul[a].y - ul[3].y));
+        e[a][2] = ((xh[a].z - xh[3].z) + (uh[a].z - uh[3].z)) + ((xl[a].z - xl[3].z) + (ul[a].z - ul[3].z));
+    }
+    const float cx = e[1][1] * e[2][2] - e[1][2] * e[2][1];
+    const float cyv = e[1][2] * e[2][0] - e[1][0] * e[2][2];
+    const float cz = e[1][0] * e[2][1] - e[1][1] * e[2][0];
+    const float w = 0.25f * fabsf(e[0][0] * cx + e[0][1] * cyv + e[0][2] * cz);
+    const float al = 0.58541020f, be = 0.13819669f;
+    float F[4][3] = {};
+#pragma unroll
+    for (int g = 0; g < 4; g++) {
+        float N[4];
+        N[0] = g == 0 ? al : be;
+        N[1] = g == 1 ? al : be;
+        N[2] = g == 2 ? al : be;
+        N[3] = 1.0f - N[0] - N[1] - N[2];
+        float r[3];
+#pragma unroll
+        for (int q = 0; q < 3; q++) r[q] = N[0] * d[0][q] + N[1] * d[1][q] + N[2] * d[2][q] + N[3] * d[3][q];
+        const float len = sqrtf(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+        const float mag = expf(-sp.k * (len - sp.radius)) / len;
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int q = 0; q < 3; q++) F[a][q] += (mag * N[a]) * r[q];
+    }
+    float fy = 0.f;
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        const float3 Fa = make_float3(w * F[a][0], w * F[a][1], w * F[a][2]);
+        fy += Fa.y;
+        if (s_cf) {
+            float4 c = s_cf[a * TILE + j];
+            c.x += Fa.x;
+            c.y += Fa.y;
+            c.z += Fa.z;
+            s_cf[a * TILE + j] = c;
+        }
+    }
+    return fy;
+}
+
+// Fixed-order sum of one float per thread of a CTA of TILE threads (shuffle tree, then the warps
+// in order by thread 0), in double; every thread must call it. Returns the total on thread 0.
+template <int TILE>
+__device__ __forceinline__ double tile_sum(float v, double* s_scratch) {
+    double x = (double)v;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0) s_scratch[threadIdx.x >> 5] = x;
+    __syncthreads();
+    double tot = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < TILE / 32; w++) tot += s_scratch[w];
+    return tot;
+}
+
 // ------------------------------------------------------------------------------------------
 // Element pass, one CTA per tile (plain loads)
 // ------------------------------------------------------------------------------------------
@@ -175,6 +268,60 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * 64))
     const MaterialDev mat = bd.cells[bd.tile_cell ? __ldg(bd.tile_cell + b) : 0].mat;
     __syncthreads();
     if (act) element_eval<MODEL, TILE>(j, t, lc, da, db, dc, pa, pb, pc, s_uh, s_ul, s_cf, s, mat, wf);
+    __syncthreads();
+    if (j < nn) node_flush<TILE>(node, reinterpret_cast<const unsigned short*>(s_inc), s_cf, s, m.np);
+}
+
+// Integrated sphere contact (InteractionSphereIntegral.cl), one CTA per tile of a cell that has
+// one; tiles of other cells return at once. SI_STEP: inside a step (time offset t_offset) — the
+// sphere's corner forces are summed per tile node in the tile's fixed incidence order and added
+// to the force accumulator like the element pass's, and on record steps of that contact the
+// tile's share of the readout (sum of the y forces) goes to tile_partials. SI_READOUT: only the
+// readout shares of contact index `contact` at the current positions (readouts between steps).
+enum SiMode : int { SI_STEP = 0, SI_READOUT = 1 };
+template <int TILE>
+__global__ void __launch_bounds__(TILE) k_si_pass(MeshDev m, StateDev s, BatchDev bd, int t_offset, int mode,
+                                                  int contact) {
+    constexpr int NMAX = TILE < TILE_NODES_MAX ? TILE : TILE_NODES_MAX;
+    __shared__ float4 s_uh[NMAX], s_ul[NMAX], s_xh[NMAX], s_xl[NMAX];
+    __shared__ float4 s_cf[4 * TILE];
+    __shared__ ushort4 s_inc[TILE];
+    __shared__ SphereIntegralStep s_sp;
+    __shared__ double s_red[TILE / 32];
+    const int b = blockIdx.x, j = threadIdx.x;
+    const CellDev& C = bd.cells[bd.tile_cell ? __ldg(bd.tile_cell + b) : 0];
+    const int si = C.si_contact;
+    if (si < 0 || (mode == SI_READOUT && si != contact)) return;  // uniform over the CTA
+    const int t = b * TILE + j;
+    const unsigned meta = __ldg(m.tile_meta + b);
+    const int ntt = (int)(meta & 0xffffu), nn = (int)(meta >> 16);
+    uint2 node = make_uint2(0u, 0u);
+    if (j < NMAX) {
+        node = m.tile_nodes[b * NMAX + j];
+        s_uh[j] = s.uh[node.x];
+        s_ul[j] = s.ul[node.x];
+        s_xh[j] = m.Xh[node.x];
+        s_xl[j] = m.Xl[node.x];
+    }
+    const uchar4 lc = m.lconn[t];
+    if (mode == SI_STEP) s_inc[j] = m.tile_inc[t];
+    const long long time = s.clock->time + (mode == SI_STEP ? t_offset : 0);
+    if (j == 0) {
+        const double cy = contact_pos(C.c[si], time);
+        const float hi = (float)cy;
+        s_sp = SphereIntegralStep{hi, (float)(cy - (double)hi), (float)C.c[si].radius, (float)C.c[si].k};
+    }
+#pragma unroll
+    for (int a = 0; a < 4; a++) s_cf[a * TILE + j] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncthreads();
+    const float fy = j < ntt ? sphere_integral<TILE>(j, lc, s_uh, s_ul, s_xh, s_xl, s_sp, s_cf) : 0.f;
+    const bool want_partial =
+        mode == SI_READOUT || (si == C.record_contact && clock_bit(s.clock->record_due, t_offset));
+    if (want_partial) {  // uniform over the CTA
+        const double tot = tile_sum<TILE>(fy, s_red);
+        if (j == 0) s.tile_partials[b] = tot;
+    }
+    if (mode != SI_STEP) return;
     __syncthreads();
     if (j < nn) node_flush<TILE>(node, reinterpret_cast<const unsigned short*>(s_inc), s_cf, s, m.np);
 }
@@ -421,6 +568,7 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 // only read for nodes that pass the coarse test.
 __device__ __forceinline__ double contact_force(const ContactDev& c, double w, const float4& xh, const float4* xlp,
                                                 const float4& uh, const float4& ul, float4& f) {
+    if (c.kind == CONTACT_SPHERE_INTEGRAL) return 0.0;  // a per-tetra force (element pass)
     // coarse test in float: nodes farther than 1e-3 from contact cannot touch
     const float yf = xh.y + uh.y;
     if (c.kind == CONTACT_SUBSTRATE) {
@@ -461,11 +609,13 @@ __device__ __forceinline__ double contact_force(const ContactDev& c, double w, c
 }
 
 // One node: element force from the fixed-point accumulator, the contacts in order (returns the
-// readout value -f_y of contact rc), and in update mode the damped velocity-Verlet step with the
-// displacement carried as hi + lo, the FIXED_TOP_BOTTOM pin, and the accumulator reset.
+// readout value -f_y of contact rc), and in update mode the cell's integrator with the
+// displacement carried as hi + lo — damped velocity Verlet with unit mass and the FIXED_TOP_BOTTOM
+// pin (VelocityVerlet.cl), or the lumped-mass form (velocityVerlet2.cl) — and the accumulator reset.
 __device__ __forceinline__ double node_step(const MeshDev& m, const StateDev& s, int i, const double* wall,
-                                           const ContactDev* cs, int nc, int rc, float vv_a, float vv_hb,
-                                           float vv_dm, int fix_a, int fix_b, bool update) {
+                                           const CellDev& C, int rc, bool update) {
+    const ContactDev* cs = C.c;
+    const int nc = C.n_contacts;
     const long long np = m.np;
     float4 f = make_float4(__ll2float_rn((long long)s.facc[i]) * FORCE_FIX_INV,
                            __ll2float_rn((long long)s.facc[np + i]) * FORCE_FIX_INV,
@@ -477,7 +627,31 @@ __device__ __forceinline__ double node_step(const MeshDev& m, const StateDev& s,
         const double fy = contact_force(cs[c], wall[c], xh, m.Xl + i, uh, ul, f);
         if (c == rc) ro = -fy;
     }
-    if (update) {
+    if (update && C.integrator == INTEGRATOR_VV2) {
+        // velocityVerlet2.cl:9-13: v = (v + (a_old + f/m)/2) / (1 + xi/2); a = f/m - xi v;
+        // x += v + a/2; the old-force slot keeps a
+        float4 v = s.v[i];
+        const float4 ao = s.fo[i];
+        const float minv = xh.w * C.inv_density;
+        const float c = C.vv2_c, xi = C.vv2_xi;
+        const float fx = f.x * minv, fy = f.y * minv, fz = f.z * minv;
+        v.x = c * (v.x + 0.5f * (ao.x + fx));
+        v.y = c * (v.y + 0.5f * (ao.y + fy));
+        v.z = c * (v.z + 0.5f * (ao.z + fz));
+        const float ax = fx - xi * v.x, ay = fy - xi * v.y, az = fz - xi * v.z;
+        df_add(uh.x, ul.x, v.x + 0.5f * ax);
+        df_add(uh.y, ul.y, v.y + 0.5f * ay);
+        df_add(uh.z, ul.z, v.z + 0.5f * az);
+        if (!isfinite(uh.x + uh.y + uh.z + v.x + v.y + v.z)) atomicOr(s.status, STATUS_NONFINITE);
+        s.uh[i] = uh;
+        s.ul[i] = ul;
+        s.v[i] = v;
+        s.fo[i] = make_float4(ax, ay, az, 0.f);
+        s.facc[i] = 0ull;
+        s.facc[np + i] = 0ull;
+        s.facc[2 * np + i] = 0ull;
+    } else if (update) {
+        const float vv_a = C.vv_a, vv_hb = C.vv_hb, vv_dm = C.vv_dm;
         float4 v = s.v[i];
         const float4 fo = s.fo[i];
         v.x = vv_a * v.x + vv_hb * (f.x + fo.x);
@@ -486,7 +660,7 @@ __device__ __forceinline__ double node_step(const MeshDev& m, const StateDev& s,
         df_add(uh.x, ul.x, vv_dm * v.x + 0.5f * f.x);
         df_add(uh.y, ul.y, vv_dm * v.y + 0.5f * f.y);
         df_add(uh.z, ul.z, vv_dm * v.z + 0.5f * f.z);
-        if (i == fix_a || i == fix_b) {  // VelocityVerlet.cl:17-22: x = z = 0
+        if (i == C.fix_a || i == C.fix_b) {  // VelocityVerlet.cl:17-22: x = z = 0
             const float4 xl = m.Xl[i];
             uh.x = -xh.x;
             ul.x = -xl.x;
@@ -545,8 +719,7 @@ __global__ void __launch_bounds__(NODE_BLOCK, NFX_NODE_MIN_BLOCKS) k_node_pass(M
     }
     double ro = 0.0;
     if (i < C.node_end)
-        ro = node_step(m, s, i, s_wall, C.c, C.n_contacts, rc, C.vv_a, C.vv_hb, C.vv_dm, C.fix_a, C.fix_b,
-                       mode == NODE_UPDATE);
+        ro = node_step(m, s, i, s_wall, C, rc, mode == NODE_UPDATE);
     if (!rec) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     ro = warp_sum_d(ro);
@@ -568,6 +741,12 @@ __global__ void __launch_bounds__(NODE_BLOCK, NFX_NODE_MIN_BLOCKS) k_node_pass(M
     const volatile double* part = s.partials;
     double acc = 0.0;
     for (int k = C.block_begin + threadIdx.x; k < C.block_end; k += NODE_BLOCK) acc += part[k];
+    if (rc >= 0 && rc == C.si_contact) {
+        // integrated sphere: -sum of the y forces, summed per tile by the element pass (or by
+        // k_si_partials for an on-demand readout)
+        const volatile double* tp = s.tile_partials;
+        for (int k = C.tile_begin + threadIdx.x; k < C.tile_end; k += NODE_BLOCK) acc -= tp[k];
+    }
     acc = warp_sum_d(acc);
     if (lane == 0) s_w[warp] = acc;
     __syncthreads();
@@ -735,6 +914,20 @@ cudaError_t launch_tet_pass(const MeshDev& m, const StateDev& s, const BatchDev&
         case 512: return launch_tile<512>(m, s, b, model, t_offset, st);
         default: return cudaErrorInvalidValue;
     }
+}
+
+cudaError_t launch_si_pass(const MeshDev& m, const StateDev& s, const BatchDev& b, int t_offset, bool readout,
+                          int contact, cudaStream_t st) {
+    if (m.ntiles <= 0) return cudaSuccess;
+    const int mode = readout ? SI_READOUT : SI_STEP;
+    switch (m.tile_tets) {
+        case 64: k_si_pass<64><<<m.ntiles, 64, 0, st>>>(m, s, b, t_offset, mode, contact); break;
+        case 128: k_si_pass<128><<<m.ntiles, 128, 0, st>>>(m, s, b, t_offset, mode, contact); break;
+        case 256: k_si_pass<256><<<m.ntiles, 256, 0, st>>>(m, s, b, t_offset, mode, contact); break;
+        case 512: k_si_pass<512><<<m.ntiles, 512, 0, st>>>(m, s, b, t_offset, mode, contact); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
 }
 
 cudaError_t launch_node_pass(const MeshDev& m, const StateDev& s, const BatchDev& b, int nblocks, int t_offset,

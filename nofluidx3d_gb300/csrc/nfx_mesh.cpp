@@ -190,8 +190,11 @@ bool build_mesh_plan(int64_t np, int64_t nt, const double* P, const uint32_t* T,
         plan.tile_node_begin[q] = (int32_t)(q * NM_);
     }
 
-    // per-tetra Dm^-1 and V0 (slot order; padding slots stay zero)
+    // per-tetra Dm^-1 and V0 (slot order; padding slots stay zero), and the lumped nodal masses of
+    // density 1 that VelocityVerlet2 uses: a quarter of every tetra's V0 to each of its corners
+    // (SimulationLegacy.py:911-924)
     plan.dmi.assign(12 * (size_t)plan.nslots, 0.0f);
+    std::vector<double> mass((size_t)np, 0.0);
     for (int64_t it = 0; it < plan.nslots; it++) {
         const int64_t ut = plan.tet_user[it];
         if (ut < 0) continue;
@@ -212,6 +215,7 @@ bool build_mesh_plan(int64_t np, int64_t nt, const double* P, const uint32_t* T,
         float* o = &plan.dmi[12 * it];
         for (int k = 0; k < 9; k++) o[k] = (float)(A[k] / det);
         o[9] = (float)(det / 6.0);
+        for (int k = 0; k < 4; k++) mass[T[k * nt + ut]] += 0.25 * (det / 6.0);
     }
 
     // reference positions, hi/lo, internal order
@@ -225,6 +229,10 @@ bool build_mesh_plan(int64_t np, int64_t nt, const double* P, const uint32_t* T,
             plan.Xh[4 * i + d] = h32;
             plan.Xl[4 * i + d] = (float)(x - (double)h32);
         }
+        // the unused fourth lane carries the inverse lumped mass (density 1); 0 for a node no
+        // tetra touches
+        const double m = mass[u];
+        plan.Xh[4 * i + 3] = m != 0.0 ? (float)(1.0 / m) : 0.0f;
     }
     return true;
 }

@@ -12,6 +12,10 @@
 //   weight grad    dW = dZ^T X          A = dZ^T[N,M]   B = X^T [K,M]   (transposed copies
 //                                                                        written by epilogues)
 // so the epilogues write activations and gradients in both layouts.
+//
+// Optional output gain: y = exp(alpha * x_k) * (W_L a + b_L) for one input k (nfx_mlp_set_output_gain).
+// With x_k the logarithm of a scale the curves are proportional to, the network itself only has
+// to learn the scale-free shape, while outputs and input gradients stay those of y.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -71,6 +75,10 @@ struct EpiArgs {
     bf16* out_b;        // [M,N]
     bf16* out_bt;       // [N,M]
     int ldo, ldot;      // leading dimensions of out and its transpose
+    const float* gain_x;  // EPI_OUTPUT: inputs [M, gain_ld]; null: no gain
+    int gain_ld, gain_k;
+    float gain_alpha;
+    const float* gain_dx;  // EPI_GRAD_INPUT: per-row term added to column gain_k; null: none
 };
 
 __device__ __forceinline__ float silu_f(float z) { return z / (1.0f + expf(-z)); }
@@ -105,7 +113,18 @@ __device__ __forceinline__ void epi_store(int epi, const EpiArgs& e, int m, int 
             e.out_bt[(size_t)n * e.ldot + m] = a;
             break;
         }
-        case EPI_OUTPUT: e.out_f[(size_t)m * e.ldo + n] = acc + e.bias[n]; break;
+        case EPI_OUTPUT: {
+            float y = acc + e.bias[n];
+            if (e.gain_x) y *= expf(e.gain_alpha * e.gain_x[(size_t)m * e.gain_ld + e.gain_k]);
+            e.out_f[(size_t)m * e.ldo + n] = y;
+            break;
+        }
+        case EPI_GRAD_INPUT: {
+            float g = acc;
+            if (e.gain_dx && n == e.gain_k) g += e.gain_dx[m];
+            e.out_f[(size_t)m * e.ldo + n] = g;
+            break;
+        }
         case EPI_GRAD_HIDDEN: {
             const bf16 g = __float2bfloat16_rn(acc * silu_grad(e.zp[(size_t)m * e.ldo + n]));
             e.out_b[(size_t)m * e.ldo + n] = g;
@@ -172,26 +191,40 @@ __global__ void k_pack_input(int M, int n_in, int kp, const float* __restrict__ 
     Xt[(size_t)k * ldt + m] = v;
 }
 
-// Weighted squared error per sample, loss_s = w_s * sum_j (y_sj - t_sj)^2, and the output
-// gradient scale * 2 w_s (y - t) as bf16 [M, N] and [N, M]. One warp per sample.
+// Weighted squared error per sample, loss_s = w_s * sum_j (y_sj - t_sj)^2, and the gradient of
+// scale * loss with respect to the last layer's output z as bf16 [M, N] and [N, M]: dL/dy =
+// scale * 2 w_s (y - t), times the row's gain exp(alpha x_k) when there is one, in which case
+// gdx[m] = alpha * sum_j y_j dL/dy_j (the gain's own input gradient) is written too. One warp
+// per sample.
 __global__ void k_loss_grad(int M, int N, const float* __restrict__ y, const float* __restrict__ tgt,
                             const float* __restrict__ w, float scale, float* __restrict__ loss, bf16* __restrict__ dy,
-                            bf16* __restrict__ dyt, int ldt) {
+                            bf16* __restrict__ dyt, int ldt, const float* __restrict__ gain_x, int gain_ld, int gain_k,
+                            float gain_alpha, float* __restrict__ gdx) {
     const int m = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (m >= M) return;
     const float ws = w ? w[m] : 1.0f;
-    float s = 0.f;
+    const float gm = gain_x ? expf(gain_alpha * gain_x[(size_t)m * gain_ld + gain_k]) : 1.0f;
+    float s = 0.f, sg = 0.f;
     for (int n = lane; n < N; n += 32) {
-        const float d = y[(size_t)m * N + n] - tgt[(size_t)m * N + n];
+        const float yv = y[(size_t)m * N + n];
+        const float d = yv - tgt[(size_t)m * N + n];
         s += d * d;
-        const bf16 g = __float2bfloat16_rn(scale * 2.0f * ws * d);
+        const float dl = scale * 2.0f * ws * d;
+        sg += yv * dl;
+        const bf16 g = __float2bfloat16_rn(dl * gm);
         dy[(size_t)m * N + n] = g;
         dyt[(size_t)n * ldt + m] = g;
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) loss[m] = ws * s;
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+        sg += __shfl_xor_sync(0xffffffffu, sg, o);
+    }
+    if (lane == 0) {
+        loss[m] = ws * s;
+        if (gain_x) gdx[m] = gain_alpha * sg;
+    }
 }
 
 // AdamW on one weight matrix [N, K] (logical columns kl of K stored, the rest padding kept at
@@ -283,6 +316,9 @@ struct nfx_mlp {
     float* y = nullptr;            // [mb, n_out]
     bf16 *dz = nullptr, *dzt = nullptr, *dz2 = nullptr, *dz2t = nullptr;  // ping-pong [mb, width]
     float* dx = nullptr;           // [mb, 16] input gradient
+    int gain_k = -1;               // output gain exp(gain_alpha * x[gain_k]); -1: none
+    float gain_alpha = 0.f;
+    float* gdx = nullptr;          // [mb] the gain's input gradient
     float* loss = nullptr;         // [mb]
     float *xin = nullptr, *tgt = nullptr, *wts = nullptr;  // staged batch inputs
     long long adam_t = 0;
@@ -317,6 +353,12 @@ int forward_dev(nfx_mlp* h, int M) {
         e.ldot = h->mb;
         if (last) {
             e.out_f = h->y;
+            if (h->gain_k >= 0) {
+                e.gain_x = h->xin;
+                e.gain_ld = h->n_in;
+                e.gain_k = h->gain_k;
+                e.gain_alpha = h->gain_alpha;
+            }
         } else {
             e.out_f = h->z[l];
             e.out_b = h->x[l + 1];
@@ -356,6 +398,10 @@ int backward_dev(nfx_mlp* h, int M, bool want_params, bool want_dx) {
             EpiArgs e{};
             e.out_f = h->dx;
             e.ldo = K;
+            if (h->gain_k >= 0) {
+                e.gain_dx = h->gdx;
+                e.gain_k = h->gain_k;
+            }
             MCUDA(gemm(h->stream, M, K, N, g, N, h->wbt[0], N, EPI_GRAD_INPUT, e));
         }
     }
@@ -371,8 +417,10 @@ int pack_input(nfx_mlp* h, int M) {
 }
 
 int loss_grad(nfx_mlp* h, int M, const float* tgt_dev, const float* w_dev, float scale) {
+    const bool gain = h->gain_k >= 0;
     k_loss_grad<<<(M + 7) / 8, 256, 0, h->stream>>>(M, h->n_out, h->y, tgt_dev, w_dev, scale, h->loss, h->dz, h->dzt,
-                                                    h->mb);
+                                                    h->mb, gain ? h->xin : nullptr, h->n_in, h->gain_k,
+                                                    h->gain_alpha, h->gdx);
     MCUDA(cudaGetLastError());
     return NFX_OK;
 }
@@ -453,7 +501,7 @@ int nfx_mlp_create(int device, int n_in, int width, int depth, int n_out, int64_
     if ((rc = malloc_dev(h, &h->y, mb * n_out)) || (rc = malloc_dev(h, &h->dz, mb * gw)) || (rc = malloc_dev(h, &h->dzt, mb * gw)) ||
         (rc = malloc_dev(h, &h->dz2, mb * gw)) || (rc = malloc_dev(h, &h->dz2t, mb * gw)) || (rc = malloc_dev(h, &h->dx, mb * 16)) ||
         (rc = malloc_dev(h, &h->loss, mb)) || (rc = malloc_dev(h, &h->xin, mb * n_in)) || (rc = malloc_dev(h, &h->tgt, mb * n_out)) ||
-        (rc = malloc_dev(h, &h->wts, mb)))
+        (rc = malloc_dev(h, &h->wts, mb)) || (rc = malloc_dev(h, &h->gdx, mb)))
         return fail_out(rc);
     // padding rows of the transposed buffers are read by the weight-gradient products: zero them
     for (void* p : {(void*)h->dz, (void*)h->dzt, (void*)h->dz2, (void*)h->dz2t})
@@ -470,6 +518,17 @@ int nfx_mlp_destroy(nfx_mlp* h) {
     for (void* p : h->allocs) cudaFree(p);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
+    return NFX_OK;
+}
+
+int nfx_mlp_set_output_gain(nfx_mlp* h, int input, float alpha) {
+    MARG(h, "null handle");
+    MARG(input >= -1 && input < h->n_in, "gain input index out of range");
+    MARG(std::isfinite(alpha), "non-finite gain exponent");
+    MCUDA(cudaSetDevice(h->device));
+    MCUDA(cudaStreamSynchronize(h->stream));
+    h->gain_k = input;
+    h->gain_alpha = input >= 0 ? alpha : 0.f;
     return NFX_OK;
 }
 

@@ -50,6 +50,11 @@ class MLP:
     def __exit__(self, *exc):
         self.close()
 
+    def set_output_gain(self, input_index: int, alpha: float) -> None:
+        """y = exp(alpha * x[input_index]) * network output; input_index -1 removes the gain."""
+        check(self._L.nfx_mlp_set_output_gain(self._h, int(input_index), C.c_float(alpha)))
+        self.gain = (int(input_index), float(alpha))
+
     @property
     def num_params(self) -> int:
         n = C.c_int64()

@@ -7,7 +7,10 @@ r mu, mu2 = (1 - r) mu), bulk/shear ratio K / mu, yield stress Y, plastic viscos
 (power-law flow with exponent 1, rate Y / eta, as workloads.Workload maps it) and the indenter
 radius Rs. The surrogate (mlp.MLP, 6 -> 256 x 3 -> 64, trained on the GPU by the package's own
 kernels) maps the inputs, scaled to [-1, 1], to the curve divided by the constant 1e-3 R^2 (the
-middle of the shear-modulus range times R^2), trained on the squared relative curve error.
+middle of the shear-modulus range times R^2), trained on the squared relative curve error. Its
+output carries the gain exp(a u_mu) = mu / 1e-3 (nfx_mlp_set_output_gain on the shear-modulus
+input), so the layers learn the curve per unit shear modulus, which varies far less across the
+box than the curve itself, while fitting the inputs still follows exact gradients of the curve.
 
 Inverse fit: given a measured curve and the known indenter radius, find the five material
 inputs. The plain method is a batched Levenberg-Marquardt on the simulator (finite-difference
@@ -193,6 +196,9 @@ class Surrogate:
         self.proto = proto
         self.net = MLP(N_IN, width, depth, proto.n_depths, max_batch=max_batch, device=device)
         self.net.set_params(_he_init(N_IN, width, depth, proto.n_depths, seed))
+        lo, hi = proto.bounds()
+        # u_mu in [-1, 1] spans log(mu) over [lo, hi]: exp(a u_mu) = mu / sqrt(lo hi) = mu / 1e-3
+        self.net.set_output_gain(0, 0.5 * math.log(hi[0] / lo[0]))
         self.history: np.ndarray | None = None
 
     def close(self) -> None:
@@ -408,9 +414,9 @@ def surrogate_fit(sur: Surrogate, targets: np.ndarray, indenter_radius: np.ndarr
 
 
 # The full experiment: a radius-16 cell (103,536 tetra), 9,600 steps per curve. The small one
-# (radius 6, 5,472 tetra, 900 steps) is for tests and quick checks.
+# (radius 8, 13,056 tetra, 2,400 steps) is for tests and quick checks.
 FULL = Protocol()
-SMALL = Protocol(radius=6.0, speed=2e-3, record_every=10, max_cells=4096)
+SMALL = Protocol(radius=8.0, speed=1e-3, record_every=20, max_cells=4096)
 
 
 def _stats(x: np.ndarray) -> dict:

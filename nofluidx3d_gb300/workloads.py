@@ -43,12 +43,15 @@ class Workload:
     C01: float = 1e-4
     yield_stress: float = 2e-4
     viscosity: float = 5e-2
-    indenter: str = "plane"     # "plane" or "sphere"
+    indenter: str = "plane"     # "plane", "sphere" or "sphere_integral" (InteractionSphereIntegral.cl)
     sphere_radius: float = 16.0
     speed: float = 1e-4
     d0: float | None = 0.0      # InitialDistance; None: top node's height - radius (see initial_distance)
     k: float = 0.1              # def_FORCE_CONST
+    si_k: float = 12.0          # PotentialForceConst of the integrated sphere contact (decay rate)
     xi: float = 1e-2            # velocity damping
+    integrator: str = "vv"      # "vv" (VelocityVerlet.cl, unit mass) or "vv2" (velocityVerlet2.cl)
+    density: float = 1.0        # lumped masses of "vv2"
     steps: int = 20000
     record_every: int = 100
     jitter: float = 0.02
@@ -94,10 +97,25 @@ class Workload:
         out = [dict(kind=0, k=self.k, radius=0.0, p0=-(R + d0), v=0.0, tmove=float("inf"))]
         if self.indenter == "plane":
             out.append(dict(kind=1, k=self.k, radius=0.0, p0=R + d0, v=self.speed, tmove=float("inf")))
-        else:
+        elif self.indenter == "sphere":
             Rs = self.sphere_radius
             out.append(dict(kind=2, k=self.k, radius=Rs, p0=R + Rs + d0, v=self.speed, tmove=float("inf")))
+        elif self.indenter == "sphere_integral":
+            Rs = self.sphere_radius
+            out.append(dict(kind=3, k=self.si_k, radius=Rs, p0=R + Rs + d0, v=self.speed, tmove=float("inf")))
+        else:
+            raise ValueError(f"unknown indenter {self.indenter!r}")
         return out
+
+    def set_integrator_on(self, target, cell=None) -> None:
+        """The integrator on a CellSim (cell None) or on one cell of a Batch."""
+        args = () if cell is None else (cell,)
+        if self.integrator == "vv2":
+            target.set_integrator_lumped(*args, self.xi, self.density)
+        elif self.integrator == "vv":
+            target.set_integrator(*args, self.xi, False)
+        else:
+            raise ValueError(f"unknown integrator {self.integrator!r}")
 
     @property
     def record_contact(self) -> int:
@@ -114,7 +132,7 @@ class Workload:
             sim.set_tetra(model, E, nu, mr)
         for c in self.contacts(m):
             sim.add_contact(c["kind"], c["k"], c["radius"], c["p0"], c["v"], c["tmove"])
-        sim.set_integrator(self.xi, False)
+        self.set_integrator_on(sim)
         rows = max_rows if max_rows is not None else self.steps // self.record_every + 1
         sim.set_record(self.record_contact, self.record_every, rows)
         return m
@@ -131,7 +149,7 @@ class Workload:
             batch.set_tetra(cell, model, E, nu, mr)
         for c in self.contacts(m):
             batch.add_contact(cell, c["kind"], c["k"], c["radius"], c["p0"], c["v"], c["tmove"])
-        batch.set_integrator(cell, self.xi, False)
+        self.set_integrator_on(batch, cell)
         return cell
 
     def with_(self, **kw) -> "Workload":

@@ -71,19 +71,25 @@ class MLPShape:
         return np.concatenate(parts).astype(np.float32)
 
 
-def forward(shape: MLPShape, p: np.ndarray, x: np.ndarray, exact: bool = False):
+def forward(shape: MLPShape, p: np.ndarray, x: np.ndarray, exact: bool = False, gain=None):
     """Returns (y, cache). exact=True: float64 without bf16 rounding (the finite-difference
-    reference); exact=False: the kernels' rounding points, float32 accumulation."""
+    reference); exact=False: the kernels' rounding points, float32 accumulation. gain = (k, alpha):
+    y = exp(alpha * x[:, k]) * last layer output, x in full precision (nfx_mlp_set_output_gain)."""
     dt = np.float64 if exact else np.float32
     rnd = (lambda a: a.astype(dt)) if exact else bf16
     layers = shape.split(p.astype(dt))
-    X = rnd(np.asarray(x, dt))
-    cache = {"X": [X], "Z": [], "W": []}
+    xf = np.asarray(x, dt)
+    X = rnd(xf)
+    cache = {"X": [X], "Z": [], "W": [], "g": None}
     for li, (W, b) in enumerate(layers):
         Wr = rnd(W)
         cache["W"].append(Wr)
         Z = (X.astype(dt) @ Wr.T.astype(dt)).astype(dt) + b.astype(dt)
         if li == len(layers) - 1:
+            if gain is not None:
+                g = np.exp(dt(gain[1]) * xf[:, gain[0]]).astype(dt)
+                cache["g"] = g
+                Z = (Z * g[:, None]).astype(dt)
             return Z, cache
         cache["Z"].append(Z)
         X = rnd(silu(Z).astype(dt))
@@ -92,17 +98,19 @@ def forward(shape: MLPShape, p: np.ndarray, x: np.ndarray, exact: bool = False):
 
 
 def loss_and_grads(shape: MLPShape, p: np.ndarray, x: np.ndarray, t: np.ndarray, w: np.ndarray | None = None,
-                   scale: float = 1.0, exact: bool = False):
+                   scale: float = 1.0, exact: bool = False, gain=None):
     """L = scale * sum_b w_b ||y_b - t_b||^2; returns (per-row losses w_b ||.||^2, dL/dp flat,
     dL/dx)."""
     dt = np.float64 if exact else np.float32
     rnd = (lambda a: a.astype(dt)) if exact else bf16
-    y, c = forward(shape, p, x, exact)
+    y, c = forward(shape, p, x, exact, gain)
     B = y.shape[0]
     wv = np.ones(B, dt) if w is None else np.asarray(w, dt)
     d = y - np.asarray(t, dt)
     rows = wv * (d * d).sum(1)
-    G = rnd((scale * 2.0 * wv[:, None] * d).astype(dt))
+    dl = (scale * 2.0 * wv[:, None] * d).astype(dt)
+    g = c["g"] if c["g"] is not None else np.ones(B, dt)
+    G = rnd((dl * g[:, None]).astype(dt))
     grads = []
     nl = len(c["W"])
     dx = None
@@ -115,7 +123,9 @@ def loss_and_grads(shape: MLPShape, p: np.ndarray, x: np.ndarray, t: np.ndarray,
         if li > 0:
             G = rnd((dX * silu_grad(c["Z"][li - 1])).astype(dt))
         else:
-            dx = dX
+            dx = dX.copy()
+            if gain is not None:
+                dx[:, gain[0]] += dt(gain[1]) * (y * dl).sum(1)
     grads.reverse()
     flat = np.concatenate([np.concatenate([gW.ravel(), gb]) for gW, gb in grads])
     return rows, flat, dx

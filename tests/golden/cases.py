@@ -45,5 +45,10 @@ CASES = {
         Case("svk_plane_R3", _w(material="nh"), 200, model=O.MODEL_SVK),
         Case("svkk_plane_R3", _w(material="nh"), 200, model=O.MODEL_SVKK),
         Case("nh_fixtb_R3", _w(material="nh"), 200, fix_top_bottom=True),
+        Case("mr_vv2_sphere_R3", _w(material="mr", indenter="sphere", sphere_radius=2.0, integrator="vv2",
+                                    xi=0.05), 300),
+        Case("mr_sphereint_R3", _w(material="mr", indenter="sphere_integral", sphere_radius=2.0, d0=0.3), 300),
+        Case("vp_sphereint_vv2_R3", _w(material="mr_vp", indenter="sphere_integral", sphere_radius=2.0, d0=0.3,
+                                       integrator="vv2", xi=0.05), 300),
     ]
 }

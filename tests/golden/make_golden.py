@@ -6,7 +6,7 @@ Simulation.timeStep (Simulation.py:232-237) and the final positions, velocities,
 force curve and (viscoplastic) plastic state are stored. The GPU box has no reference tree;
 tests there compare against these files.
 
-    python tests/golden/make_golden.py [/root/reference]
+    python tests/golden/make_golden.py [/root/reference] [case ...]
 """
 
 from __future__ import annotations
@@ -26,10 +26,12 @@ from tests.golden.cases import CASES  # noqa: E402
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
-def main(ref_root: str = "/root/reference") -> None:
+def main(ref_root: str = "/root/reference", names=None) -> None:
     if build_ref.build(ref_root) is None:
         raise SystemExit("reference tree not found")
     for name, case in CASES.items():
+        if names and name not in names:
+            continue
         st = O.State(case.problem(), "f64")
         curve = O.ref_run(st, case.steps, case.workload.record_every)
         out = dict(points=st.positions(), velocities=st.velocities(), curve=curve, steps=case.steps)
@@ -40,4 +42,4 @@ def main(ref_root: str = "/root/reference") -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", sys.argv[2:])

@@ -12,12 +12,13 @@ def oracle_problem(w: Workload, mesh=None) -> O.Problem:
     m = mesh if mesh is not None else w.mesh()
     contacts = [O.Contact(c["kind"], c["k"], p0=c["p0"], v=c["v"], tmove=min(c["tmove"], 1e300), radius=c["radius"])
                 for c in w.contacts(m)]
+    integ = dict(integrator=O.INTEGRATOR_VV2 if w.integrator == "vv2" else O.INTEGRATOR_VV, density=w.density)
     if w.material == "mr_vp":
         return O.Problem(m.points, m.tets, model=O.MODEL_VP, vp_par=w.vp_params(), contacts=contacts, xi=w.xi,
-                         record_contact=w.record_contact)
+                         record_contact=w.record_contact, **integ)
     model, E, nu, mr = w.tetra_params()
     return O.Problem(m.points, m.tets, model=model, E=E, nu=nu, mr=mr, contacts=contacts, xi=w.xi,
-                     record_contact=w.record_contact)
+                     record_contact=w.record_contact, **integ)
 
 
 def rel_traj(x_ref: np.ndarray, x: np.ndarray) -> float:

@@ -99,3 +99,33 @@ def test_batch_rejects_mixed_models():
     with pytest.raises(Exception):
         b.set_viscoplastic(c1, (1e-3, 0, 1e-2, 1, 2e-4, 4e-3, 1, 0))
     b.close()
+
+
+def test_batch_mixed_integrators_and_sphere_laws_bitwise():
+    """Lumped-mass and unit-mass integrators, node-penalty and integrated spheres in one batch:
+    each cell evolves exactly as it does alone."""
+    base = Workload("mix", radius=3.0, material="mr", speed=1e-3, record_every=50, sphere_radius=2.0)
+    cells = [base.with_(indenter="sphere", integrator="vv2", xi=0.05, seed=1),
+             base.with_(indenter="sphere_integral", d0=0.3, seed=2),
+             base.with_(indenter="sphere_integral", d0=0.3, integrator="vv2", xi=0.05, seed=3),
+             base.with_(indenter="plane", seed=4)]
+    meshes = [w.mesh() for w in cells]
+    b = Batch(0, tile_tets=128)
+    for w, m in zip(cells, meshes):
+        w.add_to_batch(b, m)
+    b.set_record(1, 50, 10)
+    b.finalize()
+    b.step(250)
+    b.record_now()
+    forces = b.indenter_force(1)
+    assert b.status() == 0
+    for i, (w, m) in enumerate(zip(cells, meshes)):
+        s = CellSim(0)
+        w.configure(s, m, max_rows=10)
+        s.step(250)
+        s.record_now()
+        assert np.array_equal(b.points(i), s.points()), i
+        assert np.array_equal(b.curve(i), s.curve()), i
+        assert forces[i] == s.indenter_force(1), i
+        s.close()
+    b.close()

@@ -109,3 +109,23 @@ def test_fit_inputs_recovers_hidden_inputs(net):
     assert np.all(x[:, 5] == x_true[:, 5])
     assert np.all(x <= 1) and np.all(x >= -1)
     assert np.median(loss) < 1e-3 * np.median(loss0)
+
+
+def test_output_gain_matches_oracle(net):
+    shape, m, p = net
+    m.set_params(p)
+    m.set_output_gain(0, 1.6)
+    try:
+        rng = np.random.default_rng(21)
+        x = rng.uniform(-1, 1, (45, 6)).astype(np.float32)
+        t = rng.normal(0, 1, (45, 64)).astype(np.float32)
+        y = m.forward(x)
+        y_ref, _ = M.forward(shape, p, x, gain=(0, 1.6))
+        assert rel(y, y_ref) < 5e-3
+        loss, dx = m.backward(x, t, scale=1.0 / 45, want_dx=True)
+        rows, g_ref, dx_ref = M.loss_and_grads(shape, p, x, t, scale=1.0 / 45, gain=(0, 1.6))
+        assert rel(loss, rows) < 5e-3
+        assert rel(m.grads(), g_ref) < 2e-2
+        assert rel(dx, dx_ref) < 2e-2
+    finally:
+        m.set_output_gain(-1, 0.0)

@@ -176,3 +176,23 @@ def test_gpu_nonfinite_input_raises_status():
     sim.step(2)
     assert sim.status() & 1
     sim.close()
+
+
+def test_sphere_integral_readout_in_step_equals_on_demand():
+    """The integrated sphere's force row at t = 100 recorded inside step 100 (tile partials from
+    the step's sphere pass) equals the row recorded between steps (its readout pass) and the
+    on-demand readout, bit for bit."""
+    w = CASES["mr_sphereint_R3"].workload
+    a, b = CellSim(0), CellSim(0)
+    w.configure(a, max_rows=10)
+    w.configure(b, max_rows=10)
+    a.step(101)
+    b.step(100)
+    b.record_now()
+    ra, rb = a.curve()[2], b.curve()[2]
+    assert ra[0] == 100 and rb[0] == 100
+    assert np.array_equal(ra, rb)
+    assert b.indenter_force(1) == rb[2]
+    assert rb[2] > 0
+    a.close()
+    b.close()

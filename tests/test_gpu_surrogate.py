@@ -1,4 +1,4 @@
-"""The learned part end to end on the small protocol (radius-6 cell, 900 steps per curve): the
+"""The learned part end to end on the small protocol (radius-8 cell, 2,400 steps per curve): the
 batched simulator generates curves, the MLP kernels train on them, and the surrogate-assisted
 inverse fit reaches the plain simulator-only fit's error with several times fewer full
 simulations. Every error is measured by the simulator, not by the network."""

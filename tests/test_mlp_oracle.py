@@ -72,3 +72,29 @@ def test_adamw_step_by_hand():
                                rtol=1e-5)
     np.testing.assert_allclose(m1, 0.1 * g, rtol=1e-6)
     np.testing.assert_allclose(v1, 0.01 * g * g, rtol=1e-5)
+
+
+def test_exact_gradients_with_output_gain():
+    shape = M.MLPShape(n_in=3, width=16, depth=2, n_out=8)
+    rng = np.random.default_rng(7)
+    p = shape.init(2).astype(np.float64)
+    x = rng.uniform(-1, 1, (4, 3))
+    t = rng.normal(0, 1, (4, 8))
+    gain = (0, 1.7)
+    _, g, dx = M.loss_and_grads(shape, p, x, t, exact=True, gain=gain)
+
+    def L(pp, xx):
+        return M.loss_and_grads(shape, pp, xx, t, exact=True, gain=gain)[0].sum()
+
+    h = 1e-6
+    for k in rng.choice(p.size, 20, replace=False):
+        e = np.zeros_like(p)
+        e[k] = h
+        fd = (L(p + e, x) - L(p - e, x)) / (2 * h)
+        assert abs(fd - g[k]) <= 1e-6 * max(1.0, abs(fd))
+    for b in range(4):
+        for k in range(3):
+            e = np.zeros_like(x)
+            e[b, k] = h
+            fd = (L(p, x + e) - L(p, x - e)) / (2 * h)
+            assert abs(fd - dx[b, k]) <= 1e-6 * max(1.0, abs(fd))
