@@ -229,6 +229,8 @@ int nfx_batch_get_curve(nfx_batch* batch, int cell, double* rows, int64_t max_ro
 /* Node positions of one cell, double[3*np] SoA in the cell's user order. */
 int nfx_batch_get_points(nfx_batch* batch, int cell, double* out);
 int nfx_batch_status(nfx_batch* batch, uint32_t* flags, int clear);
+/* The status bits of every cell, flags[cells] (the batch status is their union). */
+int nfx_batch_cell_status(nfx_batch* batch, uint32_t* flags, int clear);
 /* Cells, total tetrahedra and nodes, tile size in use. */
 int nfx_batch_info(nfx_batch* batch, int64_t* cells, int64_t* tets, int64_t* nodes, int* tile_tets);
 /* The autotuner's candidates and their times (ms for 10 steps of the sub-batch). */

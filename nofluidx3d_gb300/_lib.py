@@ -88,6 +88,7 @@ _SIGS = {
     "nfx_batch_get_curve": ([_vp, C.c_int, _vp, _i64, C.POINTER(_i64)], C.c_int),
     "nfx_batch_get_points": ([_vp, C.c_int, _vp], C.c_int),
     "nfx_batch_status": ([_vp, C.POINTER(C.c_uint32), C.c_int], C.c_int),
+    "nfx_batch_cell_status": ([_vp, _vp, C.c_int], C.c_int),
     "nfx_batch_info": ([_vp, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64), C.POINTER(C.c_int)], C.c_int),
     "nfx_batch_tuning": ([_vp, _vp, _vp, C.c_int, C.POINTER(C.c_int)], C.c_int),
     "nfx_mlp_create": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _i64, C.POINTER(_vp)], C.c_int),

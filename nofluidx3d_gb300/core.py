@@ -284,6 +284,12 @@ class Batch:
     def record_now(self) -> None:
         check(self._L.nfx_batch_record_now(self._h))
 
+    def cell_status(self, clear: bool = False) -> np.ndarray:
+        """Status bits of every cell (NFX_STATUS_*)."""
+        out = np.zeros(len(self.cells), np.uint32)
+        check(self._L.nfx_batch_cell_status(self._h, _ptr(out), int(bool(clear))))
+        return out
+
     def indenter_force(self, contact: int) -> np.ndarray:
         """Current force on contact index `contact` of every cell (0 where a cell has fewer)."""
         out = np.zeros(len(self.cells), np.float64)

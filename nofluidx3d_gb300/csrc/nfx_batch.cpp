@@ -242,7 +242,7 @@ int build_device(nfx_batch* b, const std::vector<int>& which, int tile_tets, Bat
     int* d_ttb; int* d_tnb; unsigned* d_tm; uint2* d_tn; uchar4* d_lc; ushort4* d_ti; float4 *d_da, *d_db; float2* d_dc;
     float4 *d_xh, *d_xl, *d_uh, *d_ul, *d_v, *d_fo; unsigned long long* d_fa; double* d_part; double* d_fout;
     double* d_tpart;
-    CellDev* d_cells; int *d_tc, *d_bc; unsigned* d_cc; double* d_curves = nullptr;
+    CellDev* d_cells; int *d_tc, *d_bc; unsigned* d_cc; unsigned* d_cst; double* d_curves = nullptr;
     float4 *d_pa = nullptr, *d_pb = nullptr; float2 *d_pc = nullptr, *d_fields = nullptr;
     int rc;
     const size_t rows = (size_t)std::max<long long>(b->max_rows, 1);
@@ -254,7 +254,8 @@ int build_device(nfx_batch* b, const std::vector<int>& which, int tile_tets, Bat
         (rc = balloc(A, &d_fa, 3 * (size_t)np)) || (rc = balloc(A, &d_part, nblocks)) || (rc = balloc(A, &d_fout, cells.size())) ||
         (rc = balloc(A, &d_tpart, ntiles)) ||
         (rc = balloc(A, &d_cells, cells.size())) || (rc = balloc(A, &d_tc, ntiles)) || (rc = balloc(A, &d_bc, nblocks)) ||
-        (rc = balloc(A, &d_cc, cells.size())) || (rc = balloc(A, &d_curves, 3 * rows * cells.size())) ||
+        (rc = balloc(A, &d_cc, cells.size())) || (rc = balloc(A, &d_cst, cells.size())) ||
+        (rc = balloc(A, &d_curves, 3 * rows * cells.size())) ||
         (rc = balloc(A, &D.d_clock, 1)) || (rc = balloc(A, &D.d_status, 1)))
         return rc;
     if (b->model == MODEL_VP) {
@@ -281,6 +282,7 @@ int build_device(nfx_batch* b, const std::vector<int>& which, int tile_tets, Bat
     BCUDA(cudaMemcpyAsync(d_tc, tile_cell.data(), tile_cell.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     BCUDA(cudaMemcpyAsync(d_bc, block_cell.data(), block_cell.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     BCUDA(cudaMemsetAsync(d_cc, 0, cells.size() * sizeof(unsigned), st));
+    BCUDA(cudaMemsetAsync(d_cst, 0, cells.size() * sizeof(unsigned), st));
     BCUDA(cudaMemsetAsync(d_curves, 0, 3 * rows * cells.size() * sizeof(double), st));
     BCUDA(cudaMemsetAsync(D.d_clock, 0, sizeof(StepClock), st));
     BCUDA(cudaMemsetAsync(D.d_status, 0, sizeof(unsigned), st));
@@ -328,6 +330,7 @@ int build_device(nfx_batch* b, const std::vector<int>& which, int tile_tets, Bat
     B.tile_cell = d_tc;
     B.block_cell = d_bc;
     B.cell_counter = d_cc;
+    B.cell_status = d_cst;
     B.curves = d_curves;
     B.record_every = b->record_contact >= 0 ? b->record_every : 0;
     B.max_rows = b->max_rows;
@@ -765,6 +768,17 @@ int nfx_batch_status(nfx_batch* b, uint32_t* flags, int clear) {
     if (clear) BCUDA(cudaMemsetAsync(b->dev.d_status, 0, sizeof(unsigned), b->stream));
     BCUDA(cudaStreamSynchronize(b->stream));
     *flags = h;
+    return NFX_OK;
+}
+
+int nfx_batch_cell_status(nfx_batch* b, uint32_t* flags, int clear) {
+    BARG(b && flags, "null argument");
+    if (!b->finalized) return bfail(NFX_ERR_STATE, "call nfx_batch_finalize first");
+    BCUDA(cudaSetDevice(b->device));
+    const size_t n = b->cells.size();
+    BCUDA(cudaMemcpyAsync(flags, b->dev.bd.cell_status, n * sizeof(unsigned), cudaMemcpyDeviceToHost, b->stream));
+    if (clear) BCUDA(cudaMemsetAsync(b->dev.bd.cell_status, 0, n * sizeof(unsigned), b->stream));
+    BCUDA(cudaStreamSynchronize(b->stream));
     return NFX_OK;
 }
 

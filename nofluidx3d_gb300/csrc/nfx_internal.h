@@ -168,6 +168,7 @@ struct BatchDev {
     const int* tile_cell;        // per tile; null: every tile belongs to cell 0
     const int* block_cell;       // per node block; null: every block belongs to cell 0
     unsigned* cell_counter;      // per cell: blocks finished in the readout reduction
+    unsigned* cell_status;       // per cell: status bits of that cell (null for a single simulation)
     double* curves;              // per cell: max_rows rows of (t, indentation, force)
     long long record_every;      // 0: no force recording
     long long max_rows;

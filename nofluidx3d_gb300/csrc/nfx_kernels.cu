@@ -39,6 +39,16 @@ __device__ __forceinline__ double contact_pos(const ContactDev& c, long long t) 
     return tt <= c.tmove ? c.p0 - c.v * tt : c.p0 - c.v * c.tmove;
 }
 
+// Raise status bits globally and, in a batch, on the cell they belong to (cstat may be null).
+__device__ __forceinline__ void raise_status(const StateDev& s, unsigned* cstat, unsigned bits) {
+    atomicOr(s.status, bits);
+    if (cstat) atomicOr(cstat, bits);
+}
+// The status word of tile b's cell (looked up only when a status is raised).
+__device__ __forceinline__ unsigned* tile_cell_status(const BatchDev& bd, int b) {
+    return bd.cell_status ? bd.cell_status + (bd.tile_cell ? bd.tile_cell[b] : 0) : nullptr;
+}
+
 // ------------------------------------------------------------------------------------------
 // Element pass: shared pieces
 // ------------------------------------------------------------------------------------------
@@ -46,9 +56,9 @@ __device__ __forceinline__ double contact_pos(const ContactDev& c, long long t) 
 // One tetra: displacement differences from the tile's staged node data, the material law, the
 // viscoplastic state update (written back with evict-first stores), the four corner forces
 // into the shared corner-force slots k*TILE + j (corner-major, so a warp's stores are
-// contiguous and free of bank conflicts).
+// contiguous and free of bank conflicts). Returns true when the tetra is inverted (det F <= 0).
 template <int MODEL, int TILE>
-__device__ __forceinline__ void element_eval(int j, long long t, uchar4 lc, float4 da, float4 db, float2 dc,
+__device__ __forceinline__ bool element_eval(int j, long long t, uchar4 lc, float4 da, float4 db, float2 dc,
                                              float4 pa, float4 pb, float2 pc, const float4* s_uh,
                                              const float4* s_ul, float4* s_cf, const StateDev& s,
                                              const MaterialDev& mat, bool write_fields) {
@@ -94,19 +104,20 @@ __device__ __forceinline__ void element_eval(int j, long long t, uchar4 lc, floa
         __stcs(s.vp_c + t, make_float2(P[8], eps));
         if (write_fields) __stcs(s.fields + t, make_float2(vm, pr));
     }
-    if (!(jm1 > -1.0f)) atomicOr(s.status, STATUS_INVERTED);
 #pragma unroll
     for (int k = 0; k < 4; k++) s_cf[k * TILE + j] = make_float4(f[k][0], f[k][1], f[k][2], 0.f);
+    return !(jm1 > -1.0f);
 }
 
 // One tile node: sum its corner forces in the tile's fixed incidence order and add the sum to
 // the global accumulator as 64-bit fixed point, so the total does not depend on the order in
-// which tiles finish. Incidence entries are 4*local tet + corner.
+// which tiles finish. Incidence entries are 4*local tet + corner. Returns false when the sum is
+// out of the fixed-point range (nothing is added then).
 template <int TILE>
-__device__ __forceinline__ void node_flush(uint2 node, const unsigned short* inc, const float4* s_cf,
+__device__ __forceinline__ bool node_flush(uint2 node, const unsigned short* inc, const float4* s_cf,
                                            const StateDev& s, long long np) {
     const unsigned first = node.y >> 16, count = node.y & 0xffffu;
-    if (count == 0) return;
+    if (count == 0) return true;
     float fx = 0.f, fy = 0.f, fz = 0.f;
     for (unsigned q = 0; q < count; q++) {
         const unsigned e = inc[first + q];
@@ -115,16 +126,55 @@ __device__ __forceinline__ void node_flush(uint2 node, const unsigned short* inc
         fy += c.y;
         fz += c.z;
     }
-    if (!(fabsf(fx) <= FORCE_FIX_MAX && fabsf(fy) <= FORCE_FIX_MAX && fabsf(fz) <= FORCE_FIX_MAX)) {
-        atomicOr(s.status, STATUS_NONFINITE);
-        return;
-    }
+    if (!(fabsf(fx) <= FORCE_FIX_MAX && fabsf(fy) <= FORCE_FIX_MAX && fabsf(fz) <= FORCE_FIX_MAX)) return false;
     atomicAdd(s.facc + node.x, (unsigned long long)__float2ll_rn(fx * FORCE_FIX_SCALE));
     atomicAdd(s.facc + np + node.x, (unsigned long long)__float2ll_rn(fy * FORCE_FIX_SCALE));
     atomicAdd(s.facc + 2 * np + node.x, (unsigned long long)__float2ll_rn(fz * FORCE_FIX_SCALE));
+    return true;
 }
 
 __device__ __forceinline__ bool clock_bit(const unsigned* mask, int k) { return (mask[k >> 5] >> (k & 31)) & 1u; }
+
+// Cache policy of the element pass's node-list load and node-state gathers (build-time tuning):
+// 0 streaming (evict-first) / plain, 1 read-only cached, 2 read-only with the L2 evict-last hint
+// so the node lists and displacements stay L2-resident between steps.
+#ifndef NFX_NODE_LIST_HINT
+#define NFX_NODE_LIST_HINT 0
+#endif
+#ifndef NFX_GATHER_HINT
+#define NFX_GATHER_HINT 0
+#endif
+__device__ __forceinline__ unsigned long long l2_evict_last_policy() {
+    unsigned long long pol;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+__device__ __forceinline__ uint2 load_node_entry(const uint2* p) {
+#if NFX_NODE_LIST_HINT == 1
+    return __ldg(p);
+#elif NFX_NODE_LIST_HINT == 2
+    uint2 r;
+    asm("ld.global.nc.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;"
+        : "=r"(r.x), "=r"(r.y)
+        : "l"(p), "l"(l2_evict_last_policy()));
+    return r;
+#else
+    return __ldcs(p);
+#endif
+}
+__device__ __forceinline__ float4 load_node_state(const float4* p) {
+#if NFX_GATHER_HINT == 1
+    return __ldg(p);
+#elif NFX_GATHER_HINT == 2
+    float4 r;
+    asm("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+        : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
+        : "l"(p), "l"(l2_evict_last_policy()));
+    return r;
+#else
+    return *p;
+#endif
+}
 
 // Sphere centre height, radius and decay rate of an integrated sphere contact for one step.
 struct SphereIntegralStep {
@@ -261,15 +311,17 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * 64))
     s_inc[j] = __ldcs(m.tile_inc + t);
     uint2 node = make_uint2(0u, 0u);
     if (j < NMAX) {
-        node = __ldcs(m.tile_nodes + nb + j);
-        s_uh[j] = s.uh[node.x];
-        s_ul[j] = s.ul[node.x];
+        node = load_node_entry(m.tile_nodes + nb + j);
+        s_uh[j] = load_node_state(s.uh + node.x);
+        s_ul[j] = load_node_state(s.ul + node.x);
     }
     const MaterialDev mat = bd.cells[bd.tile_cell ? __ldg(bd.tile_cell + b) : 0].mat;
     __syncthreads();
-    if (act) element_eval<MODEL, TILE>(j, t, lc, da, db, dc, pa, pb, pc, s_uh, s_ul, s_cf, s, mat, wf);
+    if (act && element_eval<MODEL, TILE>(j, t, lc, da, db, dc, pa, pb, pc, s_uh, s_ul, s_cf, s, mat, wf))
+        raise_status(s, tile_cell_status(bd, b), STATUS_INVERTED);
     __syncthreads();
-    if (j < nn) node_flush<TILE>(node, reinterpret_cast<const unsigned short*>(s_inc), s_cf, s, m.np);
+    if (j < nn && !node_flush<TILE>(node, reinterpret_cast<const unsigned short*>(s_inc), s_cf, s, m.np))
+        raise_status(s, tile_cell_status(bd, b), STATUS_NONFINITE);
 }
 
 // Integrated sphere contact (InteractionSphereIntegral.cl), one CTA per tile of a cell that has
@@ -289,7 +341,8 @@ __global__ void __launch_bounds__(TILE) k_si_pass(MeshDev m, StateDev s, BatchDe
     __shared__ SphereIntegralStep s_sp;
     __shared__ double s_red[TILE / 32];
     const int b = blockIdx.x, j = threadIdx.x;
-    const CellDev& C = bd.cells[bd.tile_cell ? __ldg(bd.tile_cell + b) : 0];
+    const int cell = bd.tile_cell ? __ldg(bd.tile_cell + b) : 0;
+    const CellDev& C = bd.cells[cell];
     const int si = C.si_contact;
     if (si < 0 || (mode == SI_READOUT && si != contact)) return;  // uniform over the CTA
     const int t = b * TILE + j;
@@ -323,7 +376,8 @@ __global__ void __launch_bounds__(TILE) k_si_pass(MeshDev m, StateDev s, BatchDe
     }
     if (mode != SI_STEP) return;
     __syncthreads();
-    if (j < nn) node_flush<TILE>(node, reinterpret_cast<const unsigned short*>(s_inc), s_cf, s, m.np);
+    if (j < nn && !node_flush<TILE>(node, reinterpret_cast<const unsigned short*>(s_inc), s_cf, s, m.np))
+        raise_status(s, bd.cell_status ? bd.cell_status + cell : nullptr, STATUS_NONFINITE);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -527,17 +581,19 @@ __global__ void __launch_bounds__(TILE) k_tet_pass_pipe(MeshDev m, StateDev s, B
                 pb = vpb[j];
                 pc = vpc[j];
             }
-            element_eval<MODEL, TILE>(j, (long long)h.tb + j, reinterpret_cast<const uchar4*>(st + StageLayout::LCONN)[j],
+            if (element_eval<MODEL, TILE>(j, (long long)h.tb + j, reinterpret_cast<const uchar4*>(st + StageLayout::LCONN)[j],
                                 reinterpret_cast<const float4*>(st + StageLayout::DMI_A)[j],
                                 reinterpret_cast<const float4*>(st + StageLayout::DMI_B)[j],
                                 reinterpret_cast<const float2*>(st + StageLayout::DMI_C)[j], pa, pb, pc,
                                 reinterpret_cast<const float4*>(st + StageLayout::UH),
-                                reinterpret_cast<const float4*>(st + StageLayout::UL), s_cf, s, mat, wf);
+                                reinterpret_cast<const float4*>(st + StageLayout::UL), s_cf, s, mat, wf))
+                atomicOr(s.status, STATUS_INVERTED);
         }
         __syncthreads();  // corner forces complete
         if (j < h.nn) {
             const uint2 node = reinterpret_cast<const uint2*>(st + StageLayout::NODES)[h.noff + j];
-            node_flush<TILE>(node, reinterpret_cast<const unsigned short*>(st + StageLayout::INC), s_cf, s, m.np);
+            if (!node_flush<TILE>(node, reinterpret_cast<const unsigned short*>(st + StageLayout::INC), s_cf, s, m.np))
+                atomicOr(s.status, STATUS_NONFINITE);
         }
         __syncthreads();  // stage `cur` and the corner forces are free again
         if (j == 0 && tile + 2 * G < m.ntiles) {
@@ -613,7 +669,7 @@ __device__ __forceinline__ double contact_force(const ContactDev& c, double w, c
 // displacement carried as hi + lo — damped velocity Verlet with unit mass and the FIXED_TOP_BOTTOM
 // pin (VelocityVerlet.cl), or the lumped-mass form (velocityVerlet2.cl) — and the accumulator reset.
 __device__ __forceinline__ double node_step(const MeshDev& m, const StateDev& s, int i, const double* wall,
-                                           const CellDev& C, int rc, bool update) {
+                                           const CellDev& C, int rc, bool update, unsigned* cstat) {
     const ContactDev* cs = C.c;
     const int nc = C.n_contacts;
     const long long np = m.np;
@@ -642,7 +698,7 @@ __device__ __forceinline__ double node_step(const MeshDev& m, const StateDev& s,
         df_add(uh.x, ul.x, v.x + 0.5f * ax);
         df_add(uh.y, ul.y, v.y + 0.5f * ay);
         df_add(uh.z, ul.z, v.z + 0.5f * az);
-        if (!isfinite(uh.x + uh.y + uh.z + v.x + v.y + v.z)) atomicOr(s.status, STATUS_NONFINITE);
+        if (!isfinite(uh.x + uh.y + uh.z + v.x + v.y + v.z)) raise_status(s, cstat, STATUS_NONFINITE);
         s.uh[i] = uh;
         s.ul[i] = ul;
         s.v[i] = v;
@@ -667,7 +723,7 @@ __device__ __forceinline__ double node_step(const MeshDev& m, const StateDev& s,
             uh.z = -xh.z;
             ul.z = -xl.z;
         }
-        if (!isfinite(uh.x + uh.y + uh.z + v.x + v.y + v.z)) atomicOr(s.status, STATUS_NONFINITE);
+        if (!isfinite(uh.x + uh.y + uh.z + v.x + v.y + v.z)) raise_status(s, cstat, STATUS_NONFINITE);
         s.uh[i] = uh;
         s.ul[i] = ul;
         s.v[i] = v;
@@ -719,7 +775,7 @@ __global__ void __launch_bounds__(NODE_BLOCK, NFX_NODE_MIN_BLOCKS) k_node_pass(M
     }
     double ro = 0.0;
     if (i < C.node_end)
-        ro = node_step(m, s, i, s_wall, C, rc, mode == NODE_UPDATE);
+        ro = node_step(m, s, i, s_wall, C, rc, mode == NODE_UPDATE, bd.cell_status ? bd.cell_status + cell : nullptr);
     if (!rec) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     ro = warp_sum_d(ro);

@@ -145,8 +145,8 @@ class SimStats:
 
 def simulate_curves(params: np.ndarray, proto: Protocol, stats: SimStats | None = None) -> np.ndarray:
     """Force at proto.depths() for every input row (one full simulation each, batched on the
-    GPU in launches of proto.max_cells cells sharing one mesh). Rows whose simulation went
-    non-finite come back as NaN."""
+    GPU in launches of proto.max_cells cells sharing one mesh). Rows whose simulation raised a
+    status (an inverted tetra, a non-finite value) come back as NaN."""
     P = np.asarray(params, np.float64).reshape(-1, N_IN)
     mesh = proto.mesh()
     depths = proto.depths()
@@ -165,10 +165,11 @@ def simulate_curves(params: np.ndarray, proto: Protocol, stats: SimStats | None 
             b.finalize()
             b.step(proto.steps)
             b.record_now()
+            bad = b.cell_status() != 0
             for i in range(chunk.shape[0]):
                 cv = b.curve(i)
                 ind, force = cv[:, 1], cv[:, 2]
-                if cv.shape[0] == rows and np.all(np.isfinite(force)):
+                if not bad[i] and cv.shape[0] == rows and np.all(np.isfinite(force)):
                     out[a + i] = np.interp(depths, ind, force)
         finally:
             b.close()

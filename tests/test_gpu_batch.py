@@ -33,6 +33,7 @@ def test_batch_equals_cells_run_alone_bitwise(monkeypatch):
     b.step(250)  # five captured 50-step graphs
     b.record_now()
     assert b.status() == 0
+    assert np.all(b.cell_status() == 0)
     for i, (w, m) in enumerate(zip(cells, meshes)):
         s = CellSim(0)
         w.configure(s, m, max_rows=10)
@@ -128,4 +129,23 @@ def test_batch_mixed_integrators_and_sphere_laws_bitwise():
         assert np.array_equal(b.curve(i), s.curve()), i
         assert forces[i] == s.indenter_force(1), i
         s.close()
+    b.close()
+
+
+def test_cell_status_marks_only_the_failing_cell():
+    """A cell that blows up physically (walls placed at +-R cut into a soft cell of non-integer
+    radius; the FP64 oracle goes non-finite too) raises its own status; its neighbour stays 0."""
+    pop = batched_cells(4, seed=7, r_range=(2.5, 4.0), steps=250)
+    good = pop[0].with_(speed=1e-3)
+    bad = pop[2].with_(speed=1e-3, d0=0.0)
+    b = Batch(0, tile_tets=128)
+    for w in (good, bad):
+        w.add_to_batch(b, w.mesh())
+    b.set_record(1, 50, 10)
+    b.finalize()
+    b.step(100)
+    st = b.cell_status()
+    assert st[0] == 0
+    assert st[1] != 0
+    assert b.status() == st[1]
     b.close()
