@@ -162,6 +162,17 @@ __device__ __forceinline__ uint2 load_node_entry(const uint2* p) {
     return __ldcs(p);
 #endif
 }
+// L2 prefetch distance of the element pass (build-time tuning; 0: off): each CTA asks the TMA
+// engine to bring the streamed arrays of tile b + NFX_PREFETCH_AHEAD into L2, so that by the time
+// a CTA starts on that tile its loads hit L2. Tiles sit at a fixed stride, so every array of a
+// tile is one contiguous, 16-byte aligned block.
+#ifndef NFX_PREFETCH_AHEAD
+#define NFX_PREFETCH_AHEAD 0
+#endif
+__device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
 __device__ __forceinline__ float4 load_node_state(const float4* p) {
 #if NFX_GATHER_HINT == 1
     return __ldg(p);
@@ -309,6 +320,22 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * 64))
         pc = __ldcs(s.vp_c + t);
     }
     s_inc[j] = __ldcs(m.tile_inc + t);
+    if (NFX_PREFETCH_AHEAD > 0 && j < 10 && b + NFX_PREFETCH_AHEAD < m.ntiles) {
+        const int q = b + NFX_PREFETCH_AHEAD;
+        const size_t o = (size_t)q * TILE;
+        switch (j) {  // one array per thread
+            case 0: prefetch_l2(m.lconn + o, 4u * TILE); break;
+            case 1: prefetch_l2(m.dmi_a + o, 16u * TILE); break;
+            case 2: prefetch_l2(m.dmi_b + o, 16u * TILE); break;
+            case 3: prefetch_l2(m.dmi_c + o, 8u * TILE); break;
+            case 4: prefetch_l2(m.tile_inc + o, 8u * TILE); break;
+            case 5: prefetch_l2(m.tile_nodes + (size_t)q * NMAX, 8u * NMAX); break;
+            case 6: if (MODEL == MODEL_VP) prefetch_l2(s.vp_a + o, 16u * TILE); break;
+            case 7: if (MODEL == MODEL_VP) prefetch_l2(s.vp_b + o, 16u * TILE); break;
+            case 8: if (MODEL == MODEL_VP) prefetch_l2(s.vp_c + o, 8u * TILE); break;
+            default: break;
+        }
+    }
     uint2 node = make_uint2(0u, 0u);
     if (j < NMAX) {
         node = load_node_entry(m.tile_nodes + nb + j);

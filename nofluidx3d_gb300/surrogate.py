@@ -66,6 +66,11 @@ class Protocol:
     mesh_seed: int = 0
     tile_tets: int = 128         # batch tile size (0: autotune)
     max_cells: int = 2048        # cells per batch launch
+    # Curves rougher than this (norm of second differences over the curve's norm; smooth curves
+    # sit near 0.02) come from cells at the explicit scheme's stability limit (stiff materials at
+    # dt = 1 with unit nodal mass, which the FP64 reference scheme cannot run either) and are
+    # discarded like cells that raised a status.
+    max_roughness: float = 0.1
 
     @property
     def max_depth(self) -> float:
@@ -146,7 +151,8 @@ class SimStats:
 def simulate_curves(params: np.ndarray, proto: Protocol, stats: SimStats | None = None) -> np.ndarray:
     """Force at proto.depths() for every input row (one full simulation each, batched on the
     GPU in launches of proto.max_cells cells sharing one mesh). Rows whose simulation raised a
-    status (an inverted tetra, a non-finite value) come back as NaN."""
+    status (an inverted tetra, a non-finite value) or whose curve is rougher than
+    proto.max_roughness come back as NaN."""
     P = np.asarray(params, np.float64).reshape(-1, N_IN)
     mesh = proto.mesh()
     depths = proto.depths()
@@ -170,7 +176,9 @@ def simulate_curves(params: np.ndarray, proto: Protocol, stats: SimStats | None 
                 cv = b.curve(i)
                 ind, force = cv[:, 1], cv[:, 2]
                 if not bad[i] and cv.shape[0] == rows and np.all(np.isfinite(force)):
-                    out[a + i] = np.interp(depths, ind, force)
+                    c = np.interp(depths, ind, force)
+                    if roughness(c) <= proto.max_roughness:
+                        out[a + i] = c
         finally:
             b.close()
     if stats is not None:
@@ -178,6 +186,12 @@ def simulate_curves(params: np.ndarray, proto: Protocol, stats: SimStats | None 
         stats.seconds += time.perf_counter() - t0
         stats.tetra_steps += float(P.shape[0]) * mesh.num_tetra * proto.steps
     return out
+
+
+def roughness(curve: np.ndarray) -> float:
+    """Norm of the second differences of a curve over its norm."""
+    c = np.asarray(curve, np.float64)
+    return float(np.linalg.norm(np.diff(c, 2)) / max(np.linalg.norm(c), 1e-300))
 
 
 def curve_error(curves: np.ndarray, targets: np.ndarray) -> np.ndarray:
@@ -450,10 +464,13 @@ def run_experiment(proto: Protocol = FULL, n_curves: int = 8192, n_hold: int = 1
     e_hold = curve_error(sur.predict(P[ho]), F[ho])
     log(f"training: {train_steps} steps in {t_train:.1f} s; held-out curve error median {np.median(e_hold):.3e}")
 
-    # noisy targets from hidden inputs
+    # noisy targets from hidden inputs (drawn until n_targets valid simulations exist: inputs past
+    # the scheme's stability limit give no curve)
     st_t = SimStats()
-    Ph = sample_params(n_targets, proto, seed + 1)
+    Ph = sample_params(int(n_targets * 1.3) + 8, proto, seed + 1)
     Fh = simulate_curves(Ph, proto, st_t)
+    valid = np.flatnonzero(np.all(np.isfinite(Fh), axis=1))[:n_targets]
+    Ph, Fh = Ph[valid], Fh[valid]
     rng = np.random.default_rng(seed)
     T = Fh * (1.0 + noise * rng.standard_normal(Fh.shape))
     good = np.all(np.isfinite(T), axis=1)

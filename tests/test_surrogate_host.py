@@ -58,3 +58,11 @@ def test_lm_fit_from_a_good_start_is_cheap():
     b = S.lm_fit(T, far, proto, max_iter=40, simulate=fake_sim)
     assert a.sims.mean() < b.sims.mean()
     assert np.median(a.error) <= np.median(b.error) + 1e-3
+
+
+def test_roughness_separates_smooth_and_jagged_curves():
+    d = np.linspace(0, 1, 64)
+    smooth = d ** 1.5
+    jag = smooth + 0.05 * (np.arange(64) % 2)
+    assert S.roughness(smooth) < 0.01
+    assert S.roughness(jag) > S.FULL.max_roughness
