@@ -218,51 +218,70 @@ METRIC = "tetra-steps/s + % HBM peak, 1 GB300"
 
 
 def run_batched(args):
-    """Batched population (256 cells, radius log-uniform in [6, 40], per-cell materials): steps/s
-    of one batch advancing every cell, against looping the plain path over the same cells (each
-    cell's plain step time measured on that cell, summed). sims/s = cells / (20k steps' time)."""
+    """Batched population (256 cells, radius log-uniform in [6, 40] unless --batch-rmin/--batch-rmax
+    say otherwise, per-cell materials): steps/s of one batch advancing every cell, against looping
+    the plain path over the same cells (each cell's plain step time measured on that cell through
+    nfx_step in CUDA-graph chunks, summed). sims/s = cells / (20k steps' time). Under torchrun the
+    cells are split across ranks by LPT on their tetra counts (no data-path collective); times are
+    the maximum over ranks."""
     from nofluidx3d_gb300.core import Batch, CellSim
+    from nofluidx3d_gb300.mesh import mesh_counts
+    from nofluidx3d_gb300.shard import lpt_partition
 
-    cells = workloads.batched_cells(args.batch_cells, seed=0)
+    world, rank, local, dist = dist_setup()
+    r_range = (args.batch_rmin, args.batch_rmax)
+    all_cells = workloads.batched_cells(args.batch_cells, seed=0, r_range=r_range)
+    n_all = len(all_cells)
+    nt_all = sum(mesh_counts(w.radius)[1] for w in all_cells)
+    mine = lpt_partition([mesh_counts(w.radius)[1] for w in all_cells], world)[rank]
+    cells = [all_cells[i] for i in mine]
     t0 = time.perf_counter()
     meshes = [w.mesh() for w in cells]
     t_mesh = time.perf_counter() - t0
-    nt = sum(m.num_tetra for m in meshes)
     t0 = time.perf_counter()
-    b = Batch(0, tile_tets=args.batch_tile)
+    b = Batch(local, tile_tets=args.batch_tile)
     for w, m in zip(cells, meshes):
         w.add_to_batch(b, m)
     b.set_record(1, 100, args.warmup + args.steps + 10)
     b.finalize()
     t_setup = time.perf_counter() - t0
-    b.time_steps(args.warmup)
-    ms = b.time_steps(args.steps)
+    b.time_steps(max(args.warmup, 50))  # at least one 50-step chunk, so its graph exists before timing
+    barrier(dist, local)
+    ms = reduce_max(dist, b.time_steps(args.steps), local)
     batch_step_ms = ms / args.steps
     status = b.status()
+    cell_status = b.cell_status()
     info = b.info()
     b.close()
     # looped plain path: each cell alone, a short timed run per cell
     plain_ms = []
     for w, m in zip(cells, meshes):
-        s = CellSim(0)
+        s = CellSim(local)
         w.configure(s, m, max_rows=4)
-        s.time_steps(10)
+        s.time_steps(100)  # warm-up that also captures the cell's 100-step graph
         plain_ms.append(s.time_steps(args.loop_steps) / args.loop_steps)
         s.close()
-    loop_step_ms = sum(plain_ms)
-    n = len(cells)
+    loop_step_ms = reduce_max(dist, sum(plain_ms), local)
+    status = int(reduce_max(dist, float(status), local))
+    n_bad = int(reduce_max(dist, float((cell_status != 0).sum()), local))
+    if rank != 0:
+        return
+    n, nt = n_all, nt_all
     sim_steps = 20000
     line = {
-        "metric": "batched sims/s (256 cells, 20k steps)", "value": n / (batch_step_ms * sim_steps / 1e3),
-        "unit": "sims/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": batch_step_ms,
+        "metric": f"batched sims/s ({n} cells, 20k steps)", "value": n / (batch_step_ms * sim_steps / 1e3),
+        "unit": "sims/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": batch_step_ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"batched {n} cells R~logU[6,40], per-cell VP materials", "tets": nt,
+        "config": {"workload": f"batched {n} cells R~logU[{r_range[0]:g},{r_range[1]:g}], per-cell VP materials",
+                   "tets": nt,
                    "tile_tets": info["tile_tets"], "autotune_ms_per_10_steps": info["tuning"],
                    "batch_tetra_steps_per_s": nt / (batch_step_ms / 1e3),
                    "looped_plain_ms_per_step": loop_step_ms,
                    "looped_plain_sims_per_s": n / (loop_step_ms * sim_steps / 1e3),
                    "speedup_vs_looped_plain": loop_step_ms / batch_step_ms,
-                   "mesh_gen_s": t_mesh, "setup_s": t_setup, "status": status},
+                   "looped_plain_steps_per_cell": args.loop_steps,
+                   "mesh_gen_s": t_mesh, "setup_s": t_setup, "status": status,
+                   "cells_with_status_max_rank": n_bad, "parallelism": f"cells sharded by LPT over {world} GPU(s)"},
     }
     print(json.dumps(line), flush=True)
 
@@ -282,7 +301,10 @@ def main():
     ap.add_argument("--batched", action="store_true", help="batched population instead of one cell")
     ap.add_argument("--batch-cells", type=int, default=256)
     ap.add_argument("--batch-tile", type=int, default=0, help="0: autotune")
-    ap.add_argument("--loop-steps", type=int, default=50)
+    ap.add_argument("--loop-steps", type=int, default=200,
+                    help="steps per cell when timing the looped plain path (multiples of 100 run as CUDA graphs)")
+    ap.add_argument("--batch-rmin", type=float, default=6.0)
+    ap.add_argument("--batch-rmax", type=float, default=40.0)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -296,13 +318,16 @@ def main():
 
     w = workloads.WORKLOADS[args.workload]()
     mesh = w.mesh()
-    total = args.warmup + args.steps + args.profile_steps + args.e2e_steps + 200
+    total = args.warmup + args.steps + args.profile_steps + args.e2e_steps + 400
     sim = CellSim(local)
     w.configure(sim, mesh, max_rows=total // w.record_every + 2)
     nt, npn = mesh.num_tetra, mesh.num_points
 
-    # warm-up (also captures the CUDA graph)
+    # warm-up; the library captures its 100-step CUDA graph on the first call of >= 100 steps, so
+    # a short warm-up is followed by one untimed 100-step chunk that captures it
     sim.time_steps(args.warmup)
+    if args.warmup < 100:
+        sim.time_steps(100)
     barrier(dist, local)
     clocks = ClockSampler(local)
     clocks.start()
