@@ -135,58 +135,6 @@ __device__ __forceinline__ bool node_flush(uint2 node, const unsigned short* inc
 
 __device__ __forceinline__ bool clock_bit(const unsigned* mask, int k) { return (mask[k >> 5] >> (k & 31)) & 1u; }
 
-// Cache policy of the element pass's node-list load and node-state gathers (build-time tuning):
-// 0 streaming (evict-first) / plain, 1 read-only cached, 2 read-only with the L2 evict-last hint
-// so the node lists and displacements stay L2-resident between steps.
-#ifndef NFX_NODE_LIST_HINT
-#define NFX_NODE_LIST_HINT 0
-#endif
-#ifndef NFX_GATHER_HINT
-#define NFX_GATHER_HINT 0
-#endif
-__device__ __forceinline__ unsigned long long l2_evict_last_policy() {
-    unsigned long long pol;
-    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
-    return pol;
-}
-__device__ __forceinline__ uint2 load_node_entry(const uint2* p) {
-#if NFX_NODE_LIST_HINT == 1
-    return __ldg(p);
-#elif NFX_NODE_LIST_HINT == 2
-    uint2 r;
-    asm("ld.global.nc.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;"
-        : "=r"(r.x), "=r"(r.y)
-        : "l"(p), "l"(l2_evict_last_policy()));
-    return r;
-#else
-    return __ldcs(p);
-#endif
-}
-// L2 prefetch distance of the element pass (build-time tuning; 0: off): each CTA asks the TMA
-// engine to bring the streamed arrays of tile b + NFX_PREFETCH_AHEAD into L2, so that by the time
-// a CTA starts on that tile its loads hit L2. Tiles sit at a fixed stride, so every array of a
-// tile is one contiguous, 16-byte aligned block.
-#ifndef NFX_PREFETCH_AHEAD
-#define NFX_PREFETCH_AHEAD 0
-#endif
-__device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes) {
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ float4 load_node_state(const float4* p) {
-#if NFX_GATHER_HINT == 1
-    return __ldg(p);
-#elif NFX_GATHER_HINT == 2
-    float4 r;
-    asm("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
-        : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
-        : "l"(p), "l"(l2_evict_last_policy()));
-    return r;
-#else
-    return *p;
-#endif
-}
-
 // Sphere centre height, radius and decay rate of an integrated sphere contact for one step.
 struct SphereIntegralStep {
     float cy_hi, cy_lo, radius, k;
@@ -320,27 +268,11 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * 64))
         pc = __ldcs(s.vp_c + t);
     }
     s_inc[j] = __ldcs(m.tile_inc + t);
-    if (NFX_PREFETCH_AHEAD > 0 && j < 10 && b + NFX_PREFETCH_AHEAD < m.ntiles) {
-        const int q = b + NFX_PREFETCH_AHEAD;
-        const size_t o = (size_t)q * TILE;
-        switch (j) {  // one array per thread
-            case 0: prefetch_l2(m.lconn + o, 4u * TILE); break;
-            case 1: prefetch_l2(m.dmi_a + o, 16u * TILE); break;
-            case 2: prefetch_l2(m.dmi_b + o, 16u * TILE); break;
-            case 3: prefetch_l2(m.dmi_c + o, 8u * TILE); break;
-            case 4: prefetch_l2(m.tile_inc + o, 8u * TILE); break;
-            case 5: prefetch_l2(m.tile_nodes + (size_t)q * NMAX, 8u * NMAX); break;
-            case 6: if (MODEL == MODEL_VP) prefetch_l2(s.vp_a + o, 16u * TILE); break;
-            case 7: if (MODEL == MODEL_VP) prefetch_l2(s.vp_b + o, 16u * TILE); break;
-            case 8: if (MODEL == MODEL_VP) prefetch_l2(s.vp_c + o, 8u * TILE); break;
-            default: break;
-        }
-    }
     uint2 node = make_uint2(0u, 0u);
     if (j < NMAX) {
-        node = load_node_entry(m.tile_nodes + nb + j);
-        s_uh[j] = load_node_state(s.uh + node.x);
-        s_ul[j] = load_node_state(s.ul + node.x);
+        node = __ldcs(m.tile_nodes + nb + j);
+        s_uh[j] = s.uh[node.x];
+        s_ul[j] = s.ul[node.x];
     }
     const MaterialDev mat = bd.cells[bd.tile_cell ? __ldg(bd.tile_cell + b) : 0].mat;
     __syncthreads();
