@@ -109,6 +109,28 @@ __device__ __forceinline__ bool element_eval(int j, long long t, uchar4 lc, floa
     return !(jm1 > -1.0f);
 }
 
+// Fixed-point value round(y) of a float y with |y| < 2^62 — equal to __float2ll_rn(y) bit for
+// bit — from two 32-bit conversions (64-bit float/integer conversions run on the FP64 pipe,
+// which is narrow on this GPU). |y| = hi 2^32 + r with hi = floor(|y| 2^-32) exact and r exact
+// in float (r < 2^32 and a multiple of ulp(|y|)); round-to-nearest-even of r equals that of |y|
+// minus hi 2^32, and the rounding is symmetric in the sign.
+__device__ __forceinline__ long long fix_round(float y) {
+    const float a = fabsf(y);
+    const unsigned hi = __float2uint_rz(a * 2.3283064365386963e-10f);  // 2^-32
+    const float r = fmaf(-(float)hi, 4294967296.0f, a);                 // exact
+    const unsigned long long v = ((unsigned long long)hi << 32) + (unsigned long long)__float2uint_rn(r);
+    return y < 0.0f ? -(long long)v : (long long)v;
+}
+
+// Float value of a fixed-point accumulator word times `scale`, from its 32-bit halves:
+// (hi 2^32 + lo) scale with one fused multiply-add (within one float rounding of the direct
+// 64-bit conversion, which would run on the FP64 pipe).
+__device__ __forceinline__ float fix_to_float(unsigned long long w, float scale) {
+    const int hi = (int)(w >> 32);
+    const unsigned lo = (unsigned)w;
+    return fmaf((float)hi * 4294967296.0f, scale, (float)lo * scale);
+}
+
 // One tile node: sum its corner forces in the tile's fixed incidence order and add the sum to
 // the global accumulator as 64-bit fixed point, so the total does not depend on the order in
 // which tiles finish. Incidence entries are 4*local tet + corner. Returns false when the sum is
@@ -127,9 +149,9 @@ __device__ __forceinline__ bool node_flush(uint2 node, const unsigned short* inc
         fz += c.z;
     }
     if (!(fabsf(fx) <= FORCE_FIX_MAX && fabsf(fy) <= FORCE_FIX_MAX && fabsf(fz) <= FORCE_FIX_MAX)) return false;
-    atomicAdd(s.facc + node.x, (unsigned long long)__float2ll_rn(fx * FORCE_FIX_SCALE));
-    atomicAdd(s.facc + np + node.x, (unsigned long long)__float2ll_rn(fy * FORCE_FIX_SCALE));
-    atomicAdd(s.facc + 2 * np + node.x, (unsigned long long)__float2ll_rn(fz * FORCE_FIX_SCALE));
+    atomicAdd(s.facc + node.x, (unsigned long long)fix_round(fx * FORCE_FIX_SCALE));
+    atomicAdd(s.facc + np + node.x, (unsigned long long)fix_round(fy * FORCE_FIX_SCALE));
+    atomicAdd(s.facc + 2 * np + node.x, (unsigned long long)fix_round(fz * FORCE_FIX_SCALE));
     return true;
 }
 
@@ -233,8 +255,11 @@ __device__ __forceinline__ double tile_sum(float v, double* s_scratch) {
 // ------------------------------------------------------------------------------------------
 // The tile's material comes from its cell's entry in the cell table (cell 0 when the table has
 // no tile map), so a single simulation and a batch run this same code.
+#ifndef NFX_TET_REGS
+#define NFX_TET_REGS 64  // registers per thread the element pass is compiled for (8 CTAs of 128 per SM)
+#endif
 template <int MODEL, int TILE>
-__global__ void __launch_bounds__(TILE, 65536 / (TILE * 64))
+__global__ void __launch_bounds__(TILE, 65536 / (TILE * NFX_TET_REGS))
     k_tet_pass(MeshDev m, StateDev s, BatchDev bd, int t_offset) {
     constexpr int NMAX = TILE < TILE_NODES_MAX ? TILE : TILE_NODES_MAX;
     __shared__ float4 s_uh[NMAX];
@@ -632,9 +657,8 @@ __device__ __forceinline__ double node_step(const MeshDev& m, const StateDev& s,
     const ContactDev* cs = C.c;
     const int nc = C.n_contacts;
     const long long np = m.np;
-    float4 f = make_float4(__ll2float_rn((long long)s.facc[i]) * FORCE_FIX_INV,
-                           __ll2float_rn((long long)s.facc[np + i]) * FORCE_FIX_INV,
-                           __ll2float_rn((long long)s.facc[2 * np + i]) * FORCE_FIX_INV, 0.f);
+    float4 f = make_float4(fix_to_float(s.facc[i], FORCE_FIX_INV), fix_to_float(s.facc[np + i], FORCE_FIX_INV),
+                           fix_to_float(s.facc[2 * np + i], FORCE_FIX_INV), 0.f);
     const float4 xh = m.Xh[i];
     float4 uh = s.uh[i], ul = s.ul[i];
     double ro = 0.0;
