@@ -603,16 +603,25 @@ __device__ __forceinline__ double warp_sum_d(double v) {
     return v;
 }
 
+// A contact's values for one step, shared by a node block: the position in double for the
+// exact formulas, and in float (with the sphere radius) for the coarse test every node runs, so
+// that no node converts a double (conversions run on the FP64 pipe).
+struct WallStep {
+    double w;
+    float wf, rf;
+};
+
 // Contact force on one node in double precision (the reference's FP64 formulas). Returns the
 // y component for the readout; adds the force to f. The low part of the reference position is
 // only read for nodes that pass the coarse test.
-__device__ __forceinline__ double contact_force(const ContactDev& c, double w, const float4& xh, const float4* xlp,
-                                                const float4& uh, const float4& ul, float4& f) {
+__device__ __forceinline__ double contact_force(const ContactDev& c, const WallStep& ws, const float4& xh,
+                                                const float4* xlp, const float4& uh, const float4& ul, float4& f) {
     if (c.kind == CONTACT_SPHERE_INTEGRAL) return 0.0;  // a per-tetra force (element pass)
+    const double w = ws.w;
     // coarse test in float: nodes farther than 1e-3 from contact cannot touch
     const float yf = xh.y + uh.y;
     if (c.kind == CONTACT_SUBSTRATE) {
-        if ((float)w - yf < -1e-3f) return 0.0;
+        if (ws.wf - yf < -1e-3f) return 0.0;
         const float4 xl = *xlp;
         const double y = ((double)xh.y + (double)xl.y) + ((double)uh.y + (double)ul.y);
         const double dis = fmax(w - y, 0.0);
@@ -621,7 +630,7 @@ __device__ __forceinline__ double contact_force(const ContactDev& c, double w, c
         return fy;
     }
     if (c.kind == CONTACT_PLANE) {
-        if (yf - (float)w < -1e-3f) return 0.0;
+        if (yf - ws.wf < -1e-3f) return 0.0;
         const float4 xl = *xlp;
         const double y = ((double)xh.y + (double)xl.y) + ((double)uh.y + (double)ul.y);
         const double dis = fmax(y - w, 0.0);
@@ -630,8 +639,8 @@ __device__ __forceinline__ double contact_force(const ContactDev& c, double w, c
         return fy;
     }
     // sphere centred at (0, w, 0)
-    const float rxf = xh.x + uh.x, ryf = yf - (float)w, rzf = xh.z + uh.z;
-    const float rr = (float)c.radius + 1e-3f;
+    const float rxf = xh.x + uh.x, ryf = yf - ws.wf, rzf = xh.z + uh.z;
+    const float rr = ws.rf + 1e-3f;
     if (rxf * rxf + ryf * ryf + rzf * rzf > rr * rr) return 0.0;
     const float4 xl = *xlp;
     const double rx = ((double)xh.x + (double)xl.x) + ((double)uh.x + (double)ul.x);
@@ -652,7 +661,7 @@ __device__ __forceinline__ double contact_force(const ContactDev& c, double w, c
 // readout value -f_y of contact rc), and in update mode the cell's integrator with the
 // displacement carried as hi + lo — damped velocity Verlet with unit mass and the FIXED_TOP_BOTTOM
 // pin (VelocityVerlet.cl), or the lumped-mass form (velocityVerlet2.cl) — and the accumulator reset.
-__device__ __forceinline__ double node_step(const MeshDev& m, const StateDev& s, int i, const double* wall,
+__device__ __forceinline__ double node_step(const MeshDev& m, const StateDev& s, int i, const WallStep* wall,
                                            const CellDev& C, int rc, bool update, unsigned* cstat) {
     const ContactDev* cs = C.c;
     const int nc = C.n_contacts;
@@ -729,7 +738,7 @@ __device__ __forceinline__ double node_step(const MeshDev& m, const StateDev& s,
 __global__ void __launch_bounds__(NODE_BLOCK, NFX_NODE_MIN_BLOCKS) k_node_pass(MeshDev m, StateDev s, BatchDev bd, int t_offset, int mode,
                                                           int readout_contact) {
     __shared__ double s_w[NODE_BLOCK / 32];
-    __shared__ double s_wall[MAX_CONTACTS];
+    __shared__ WallStep s_wall[MAX_CONTACTS];
     __shared__ int s_last;
     const int cell = bd.block_cell ? __ldg(bd.block_cell + blockIdx.x) : 0;
     const CellDev& C = bd.cells[cell];
@@ -737,7 +746,10 @@ __global__ void __launch_bounds__(NODE_BLOCK, NFX_NODE_MIN_BLOCKS) k_node_pass(M
     const long long t = s.clock->time + t_offset;
     // the cell's contact positions at time t, once per block (FP64 and table lookups stay off the
     // per-node path)
-    if (threadIdx.x < C.n_contacts) s_wall[threadIdx.x] = contact_pos(C.c[threadIdx.x], t);
+    if (threadIdx.x < C.n_contacts) {
+        const double w = contact_pos(C.c[threadIdx.x], t);
+        s_wall[threadIdx.x] = WallStep{w, (float)w, (float)C.c[threadIdx.x].radius};
+    }
     __syncthreads();
     int rc;
     bool rec;
@@ -797,7 +809,7 @@ __global__ void __launch_bounds__(NODE_BLOCK, NFX_NODE_MIN_BLOCKS) k_node_pass(M
         } else {
             double* r = bd.curves + 3 * ((long long)cell * bd.max_rows + row);
             r[0] = (double)t;
-            r[1] = contact_pos(C.c[rc], 0) - s_wall[rc];
+            r[1] = contact_pos(C.c[rc], 0) - s_wall[rc].w;
             r[2] = tot;
         }
         bd.cell_counter[cell] = 0u;
