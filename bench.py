@@ -13,7 +13,10 @@ descending 1e-4 per step, damping 1e-2, FP32 kernels. A "step" is one time step 
              per-step beforeTimeStep callable) and node positions plus the force row are read
              back into pinned host memory (the reference's writeVTK readback).
   roofline   the element pass (dominant kernel): algorithmic bytes per launch / its average
-             CUDA-event duration (nfx_profile_steps), against MEASURED_PEAKS.json hbm_gbs.
+             launch duration, from --tet-launches back-to-back launches between two CUDA events
+             (nfx_profile_tet_pass), against MEASURED_PEAKS.json hbm_gbs. The per-step
+             launch-by-launch event profile (nfx_profile_steps) is reported beside it in config;
+             its brackets add the event overhead to every kernel.
   cpu_baseline  the oracle port of the reference kernels (FP64, OpenMP, all host cores) on a
              bounded sample of the same workload.
 
@@ -294,6 +297,8 @@ def main():
     ap.add_argument("--impl", default="nfx", choices=["nfx", "reference"])
     ap.add_argument("--workload", default="plain-large", choices=sorted(workloads.WORKLOADS))
     ap.add_argument("--profile-steps", type=int, default=20)
+    ap.add_argument("--tet-launches", type=int, default=20,
+                    help="back-to-back element-pass launches timed for the roofline")
     ap.add_argument("--e2e-steps", type=int, default=1000)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--reference-seconds", type=float, default=90.0)
@@ -337,11 +342,13 @@ def main():
     ms = reduce_max(dist, ms, local)
     value = world * nt * args.steps / (ms / 1e3)
 
-    # per-kernel CUDA-event profile of the element and node passes
+    # per-kernel CUDA-event profile of the element and node passes, then the element pass alone
+    # over back-to-back launches (its effects undone)
     tet_ms, node_ms = sim.profile_steps(args.profile_steps)
     tet_avg = tet_ms / args.profile_steps
+    tet_launch_ms = sim.profile_tet_pass(args.tet_launches)
     elem_bytes = ELEM_BYTES[w.material] * nt
-    achieved = elem_bytes / (tet_avg / 1e3) / 1e9
+    achieved = elem_bytes / (tet_launch_ms / 1e3) / 1e9
     peaks = load_peaks()
     traffic_per_tet = load_traffic(args.workload)
 
@@ -390,10 +397,11 @@ def main():
                          "of algorithmic state streamed per step vs 129 MB L2",
                    "step_bytes_per_tetra": ELEM_BYTES[w.material] + NODE_BYTES * npn / nt,
                    "step_gbs": (ELEM_BYTES[w.material] * nt + NODE_BYTES * npn) / (ms / args.steps / 1e3) / 1e9,
-                   "tet_pass_ms": tet_avg, "node_pass_ms": node_ms / args.profile_steps, "status": status},
+                   "tet_pass_ms": tet_launch_ms, "tet_pass_ms_bracketed": tet_avg,
+                   "node_pass_ms_bracketed": node_ms / args.profile_steps, "status": status},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
-                     "kernel": "k_tet_pass (element pass)",
+                     "kernel": "k_tet_pass (element pass)", "launches_timed": args.tet_launches,
                      "algorithmic_bytes_per_launch": elem_bytes,
                      "traffic": None if traffic_per_tet is None else traffic_per_tet * nt},
         "cpu_baseline": cpu,

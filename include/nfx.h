@@ -179,6 +179,12 @@ int nfx_time_steps(nfx_sim* sim, int64_t nsteps, float* ms);
  * summed device time of the element passes (*tet_ms) and node passes (*node_ms). */
 int nfx_profile_steps(nfx_sim* sim, int64_t nsteps, float* tet_ms, float* node_ms);
 
+/* Average device time of one element pass (*ms), from `launches` back-to-back launches of the
+ * pass for the current step between two CUDA events on the handle's stream. The passes' effects
+ * (accumulated forces and, for the viscoplastic law, the plastic state and stress fields) are
+ * undone before return. A timing helper with no counterpart in the reference. */
+int nfx_profile_tet_pass(nfx_sim* sim, int launches, float* ms);
+
 /* Number of mesh tiles and distinct-node entries (diagnostics for the tile layout). */
 int nfx_mesh_info(nfx_sim* sim, int64_t* ntiles, int64_t* tile_nodes);
 

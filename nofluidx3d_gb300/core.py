@@ -204,6 +204,13 @@ class CellSim:
         check(self._L.nfx_profile_steps(self._h, int(n), C.byref(a), C.byref(b)))
         return a.value, b.value
 
+    def profile_tet_pass(self, launches: int) -> float:
+        """Average device ms of one element pass over `launches` back-to-back launches (its
+        effects on the state are undone)."""
+        ms = C.c_float()
+        check(self._L.nfx_profile_tet_pass(self._h, int(launches), C.byref(ms)))
+        return ms.value
+
     def mesh_info(self) -> tuple[int, int]:
         a, b = C.c_int64(), C.c_int64()
         check(self._L.nfx_mesh_info(self._h, C.byref(a), C.byref(b)))

@@ -826,6 +826,66 @@ int nfx_profile_steps(nfx_sim* s, int64_t nsteps, float* tet_ms, float* node_ms)
     return NFX_OK;
 }
 
+int nfx_profile_tet_pass(nfx_sim* s, int launches, float* ms) {
+    CHECK_ARG(s && ms, "null argument");
+    CHECK_ARG(launches >= 1 && launches <= 4096, "launch count out of range [1, 4096]");
+    int rc;
+    if ((rc = require_ready(s)) != NFX_OK) return rc;
+    if ((rc = set_device(s)) != NFX_OK) return rc;
+    if ((rc = upload_cell(s)) != NFX_OK) return rc;
+    // The element pass advances the plastic state (and may write the stress fields): keep a copy
+    // of both and put it back afterwards.
+    const bool vp = s->cell.mat.model == MODEL_VP && s->st.vp_a;
+    const size_t ntp = (size_t)s->plan.nslots + ARRAY_PAD;
+    std::vector<void*> keep;
+    auto release = [&]() {
+        for (void* q : keep) cudaFree(q);
+    };
+    if (vp) {
+        const void* src[4] = {s->st.vp_a, s->st.vp_b, s->st.vp_c, s->st.fields};
+        const size_t bytes[4] = {ntp * sizeof(float4), ntp * sizeof(float4), ntp * sizeof(float2), ntp * sizeof(float2)};
+        for (int i = 0; i < 4; i++) {
+            void* q = nullptr;
+            cudaError_t e = cudaMalloc(&q, bytes[i]);
+            if (e != cudaSuccess) {
+                release();
+                return fail(NFX_ERR_NOMEM, std::string("profile_tet_pass: cudaMalloc: ") + cudaGetErrorString(e));
+            }
+            keep.push_back(q);
+            e = cudaMemcpyAsync(q, src[i], bytes[i], cudaMemcpyDeviceToDevice, s->stream);
+            if (e != cudaSuccess) {
+                release();
+                return fail(NFX_ERR_CUDA, std::string("profile_tet_pass: save: ") + cudaGetErrorString(e));
+            }
+        }
+    }
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t err = cudaEventCreate(&e0);
+    if (err == cudaSuccess) err = cudaEventCreate(&e1);
+    if (err == cudaSuccess) err = cudaEventRecord(e0, s->stream);
+    for (int k = 0; k < launches && err == cudaSuccess; k++) err = launch_elem(s, 0);
+    if (err == cudaSuccess) err = cudaEventRecord(e1, s->stream);
+    float t = 0.f;
+    if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+    if (err == cudaSuccess) err = cudaEventElapsedTime(&t, e0, e1);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    // Undo the passes' effects: the accumulated forces and, for the viscoplastic law, the state.
+    if (err == cudaSuccess)
+        err = cudaMemsetAsync(s->st.facc, 0, 3 * (size_t)s->mesh.np * sizeof(unsigned long long), s->stream);
+    if (vp && err == cudaSuccess) {
+        void* dst[4] = {s->st.vp_a, s->st.vp_b, s->st.vp_c, s->st.fields};
+        const size_t bytes[4] = {ntp * sizeof(float4), ntp * sizeof(float4), ntp * sizeof(float2), ntp * sizeof(float2)};
+        for (int i = 0; i < 4 && err == cudaSuccess; i++)
+            err = cudaMemcpyAsync(dst[i], keep[i], bytes[i], cudaMemcpyDeviceToDevice, s->stream);
+    }
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s->stream);
+    release();
+    if (err != cudaSuccess) return fail(NFX_ERR_CUDA, std::string("profile_tet_pass: ") + cudaGetErrorString(err));
+    *ms = t / (float)launches;
+    return NFX_OK;
+}
+
 int nfx_mesh_info(nfx_sim* s, int64_t* ntiles, int64_t* tile_nodes) {
     CHECK_ARG(s && ntiles && tile_nodes, "null argument");
     if (!s->have_mesh) return fail(NFX_ERR_STATE, "no mesh");

@@ -122,13 +122,27 @@ __device__ __forceinline__ long long fix_round(float y) {
     return y < 0.0f ? -(long long)v : (long long)v;
 }
 
-// Float value of a fixed-point accumulator word times `scale`, from its 32-bit halves:
-// (hi 2^32 + lo) scale with one fused multiply-add (within one float rounding of the direct
-// 64-bit conversion, which would run on the FP64 pipe).
-__device__ __forceinline__ float fix_to_float(unsigned long long w, float scale) {
-    const int hi = (int)(w >> 32);
-    const unsigned lo = (unsigned)w;
-    return fmaf((float)hi * 4294967296.0f, scale, (float)lo * scale);
+// Float value of a fixed-point accumulator word, w 2^-40 rounded to nearest even — bit for bit
+// __ll2float_rn(w) * 2^-40 — built from integer operations alone: normalise |w| with a count
+// of leading zeros, keep 24 bits, round on the 40 bits below, and assemble sign, exponent and
+// mantissa (the float conversions, 64- and 32-bit alike, run on the narrow FP64 pipe).
+__device__ __forceinline__ float fix_to_float(unsigned long long w) {
+    const long long sw = (long long)w;
+    if (sw == 0) return 0.0f;
+    const unsigned sign = sw < 0 ? 0x80000000u : 0u;
+    unsigned long long a = sw < 0 ? 0ull - w : w;
+    const int lz = __clzll((long long)a);
+    a <<= lz;  // leading one at bit 63
+    unsigned long long m = a >> 40;  // 24 significant bits
+    const unsigned long long rem = a & ((1ull << 40) - 1ull), half = 1ull << 39;
+    if (rem > half || (rem == half && (m & 1ull))) m++;
+    int e = 63 - lz;  // |w| in [2^e, 2^(e+1))
+    if (m == (1ull << 24)) {
+        m >>= 1;
+        e++;
+    }
+    const unsigned be = (unsigned)(e - 40 + 127);  // times 2^-40; always a normal float
+    return __uint_as_float(sign | (be << 23) | ((unsigned)m & 0x7FFFFFu));
 }
 
 // One tile node: sum its corner forces in the tile's fixed incidence order and add the sum to
@@ -666,8 +680,7 @@ __device__ __forceinline__ double node_step(const MeshDev& m, const StateDev& s,
     const ContactDev* cs = C.c;
     const int nc = C.n_contacts;
     const long long np = m.np;
-    float4 f = make_float4(fix_to_float(s.facc[i], FORCE_FIX_INV), fix_to_float(s.facc[np + i], FORCE_FIX_INV),
-                           fix_to_float(s.facc[2 * np + i], FORCE_FIX_INV), 0.f);
+    float4 f = make_float4(fix_to_float(s.facc[i]), fix_to_float(s.facc[np + i]), fix_to_float(s.facc[2 * np + i]), 0.f);
     const float4 xh = m.Xh[i];
     float4 uh = s.uh[i], ul = s.ul[i];
     double ro = 0.0;
