@@ -58,7 +58,7 @@ struct MeshPlan {
     std::vector<uint32_t> tile_nodes;      // 2 per node entry: internal node id, (first << 16 | count)
                                            // of its run in the tile's incidence list
     std::vector<uint8_t> lconn;            // 4 * nslots local corner indices
-    std::vector<uint16_t> tile_inc;        // 4 * nslots: per tile, the corners (4*local tet + corner)
+    std::vector<uint16_t> tile_inc;        // 4 * nslots: per tile, the corners (corner * tile size + local tet)
                                            // grouped by local node in node order, tet order within
     std::vector<float> dmi;                // 12 * nslots: Dm^-1 row-major (9), V0, pad, pad
     std::vector<float> Xh, Xl;             // 4 * np: reference position hi / lo parts; Xh.w holds the

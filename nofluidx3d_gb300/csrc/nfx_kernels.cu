@@ -147,17 +147,31 @@ __device__ __forceinline__ float fix_to_float(unsigned long long w) {
 
 // One tile node: sum its corner forces in the tile's fixed incidence order and add the sum to
 // the global accumulator as 64-bit fixed point, so the total does not depend on the order in
-// which tiles finish. Incidence entries are 4*local tet + corner. Returns false when the sum is
-// out of the fixed-point range (nothing is added then).
+// which tiles finish. Incidence entries are corner-force slots (corner * TILE + local tet). The
+// loop takes four corners per iteration (their loads issued together; 2.7 % faster element pass
+// than one at a time at R = 64), adding them in list order all the same. Returns false when the
+// sum is out of the fixed-point range (nothing is added then).
+#ifndef NFX_FLUSH_UNROLL
+#define NFX_FLUSH_UNROLL 4  // 1: one corner per iteration
+#endif
 template <int TILE>
 __device__ __forceinline__ bool node_flush(uint2 node, const unsigned short* inc, const float4* s_cf,
                                            const StateDev& s, long long np) {
     const unsigned first = node.y >> 16, count = node.y & 0xffffu;
     if (count == 0) return true;
+    const unsigned short* e = inc + first;
     float fx = 0.f, fy = 0.f, fz = 0.f;
-    for (unsigned q = 0; q < count; q++) {
-        const unsigned e = inc[first + q];
-        const float4 c = s_cf[(e & 3u) * TILE + (e >> 2)];
+    unsigned q = 0;
+#if NFX_FLUSH_UNROLL == 4
+    for (; q + 4 <= count; q += 4) {
+        const float4 c0 = s_cf[e[q]], c1 = s_cf[e[q + 1]], c2 = s_cf[e[q + 2]], c3 = s_cf[e[q + 3]];
+        fx = (((fx + c0.x) + c1.x) + c2.x) + c3.x;
+        fy = (((fy + c0.y) + c1.y) + c2.y) + c3.y;
+        fz = (((fz + c0.z) + c1.z) + c2.z) + c3.z;
+    }
+#endif
+    for (; q < count; q++) {
+        const float4 c = s_cf[e[q]];
         fx += c.x;
         fy += c.y;
         fz += c.z;
@@ -272,6 +286,35 @@ __device__ __forceinline__ double tile_sum(float v, double* s_scratch) {
 #ifndef NFX_TET_REGS
 #define NFX_TET_REGS 64  // registers per thread the element pass is compiled for (8 CTAs of 128 per SM)
 #endif
+#ifndef NFX_DMI_FROM_X
+#define NFX_DMI_FROM_X 0  // 1: Dm^-1 and V0 from the staged reference positions instead of the stored arrays
+#endif
+
+// Dm^-1 (row-major, in the stored arrays' layout) and V0 = det(Dm)/6 of one tetra from its
+// corners' reference positions X = Xh + Xl staged in shared memory: Dm's columns are the edges
+// X_k - X_0 (hi and lo parts differenced separately), the inverse is adj(Dm)/det(Dm) with a
+// correctly rounded reciprocal — the host's construction in float.
+__device__ __forceinline__ void ref_shape_inverse(uchar4 lc, const float4* s_xh, const float4* s_xl, float4& da,
+                                                  float4& db, float2& dc) {
+    const float4 h0 = s_xh[lc.x], l0 = s_xl[lc.x];
+    const int lk[3] = {lc.y, lc.z, lc.w};
+    float M[9];  // M[3 d + k] = X_(k+1),d - X_0,d
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const float4 h = s_xh[lk[k]], l = s_xl[lk[k]];
+        M[k] = (h.x - h0.x) + (l.x - l0.x);
+        M[3 + k] = (h.y - h0.y) + (l.y - l0.y);
+        M[6 + k] = (h.z - h0.z) + (l.z - l0.z);
+    }
+    const float A0 = M[4] * M[8] - M[5] * M[7], A1 = M[2] * M[7] - M[1] * M[8], A2 = M[1] * M[5] - M[2] * M[4];
+    const float A3 = M[5] * M[6] - M[3] * M[8], A4 = M[0] * M[8] - M[2] * M[6], A5 = M[2] * M[3] - M[0] * M[5];
+    const float A6 = M[3] * M[7] - M[4] * M[6], A7 = M[1] * M[6] - M[0] * M[7], A8 = M[0] * M[4] - M[1] * M[3];
+    const float det = M[0] * A0 + M[1] * A3 + M[2] * A6;
+    const float r = __frcp_rn(det);
+    da = make_float4(A0 * r, A1 * r, A2 * r, A3 * r);
+    db = make_float4(A4 * r, A5 * r, A6 * r, A7 * r);
+    dc = make_float2(A8 * r, det * (1.0f / 6.0f));
+}
 template <int MODEL, int TILE>
 __global__ void __launch_bounds__(TILE, 65536 / (TILE * NFX_TET_REGS))
     k_tet_pass(MeshDev m, StateDev s, BatchDev bd, int t_offset) {
@@ -280,6 +323,10 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * NFX_TET_REGS))
     __shared__ float4 s_ul[NMAX];
     __shared__ float4 s_cf[4 * TILE];  // corner forces, slot corner*TILE + local tet
     __shared__ ushort4 s_inc[TILE];    // the tile's incidence list
+#if NFX_DMI_FROM_X
+    __shared__ float4 s_xh[NMAX];
+    __shared__ float4 s_xl[NMAX];
+#endif
 
     const int b = blockIdx.x;
     const int j = threadIdx.x;
@@ -296,9 +343,11 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * NFX_TET_REGS))
     // Streaming per-tetra data (read once per step: evict-first) and the node list, issued for
     // every slot and entry without waiting for the meta word: padding is valid zeroed memory.
     const uchar4 lc = __ldcs(m.lconn + t);
+#if !NFX_DMI_FROM_X
     const float4 da = __ldcs(m.dmi_a + t);
     const float4 db = __ldcs(m.dmi_b + t);
     const float2 dc = __ldcs(m.dmi_c + t);
+#endif
     float4 pa = make_float4(0.f, 0.f, 0.f, 0.f), pb = pa;
     float2 pc = make_float2(0.f, 0.f);
     if (MODEL == MODEL_VP) {
@@ -312,9 +361,18 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * NFX_TET_REGS))
         node = __ldcs(m.tile_nodes + nb + j);
         s_uh[j] = s.uh[node.x];
         s_ul[j] = s.ul[node.x];
+#if NFX_DMI_FROM_X
+        s_xh[j] = m.Xh[node.x];
+        s_xl[j] = m.Xl[node.x];
+#endif
     }
     const MaterialDev mat = bd.cells[bd.tile_cell ? __ldg(bd.tile_cell + b) : 0].mat;
     __syncthreads();
+#if NFX_DMI_FROM_X
+    float4 da = make_float4(0.f, 0.f, 0.f, 0.f), db = da;
+    float2 dc = make_float2(0.f, 0.f);
+    if (act) ref_shape_inverse(lc, s_xh, s_xl, da, db, dc);
+#endif
     if (act && element_eval<MODEL, TILE>(j, t, lc, da, db, dc, pa, pb, pc, s_uh, s_ul, s_cf, s, mat, wf))
         raise_status(s, tile_cell_status(bd, b), STATUS_INVERTED);
     __syncthreads();
@@ -625,50 +683,51 @@ struct WallStep {
     float wf, rf;
 };
 
-// Contact force on one node in double precision (the reference's FP64 formulas). Returns the
-// y component for the readout; adds the force to f. The low part of the reference position is
-// only read for nodes that pass the coarse test.
-__device__ __forceinline__ double contact_force(const ContactDev& c, const WallStep& ws, const float4& xh,
-                                                const float4* xlp, const float4& uh, const float4& ul, float4& f) {
-    if (c.kind == CONTACT_SPHERE_INTEGRAL) return 0.0;  // a per-tetra force (element pass)
+// Contact force on one node in double precision (the reference's FP64 formulas). Returns false
+// for a node out of contact (no force); otherwise adds the force to f and returns its y component
+// in fy for the readout. Only nodes that pass the coarse float test read the low part of the
+// reference position or do any double arithmetic (the FP64 pipe is narrow on this GPU).
+__device__ __forceinline__ bool contact_force(const ContactDev& c, const WallStep& ws, const float4& xh,
+                                              const float4* xlp, const float4& uh, const float4& ul, float4& f,
+                                              double& fy) {
+    if (c.kind == CONTACT_SPHERE_INTEGRAL) return false;  // a per-tetra force (element pass)
     const double w = ws.w;
     // coarse test in float: nodes farther than 1e-3 from contact cannot touch
     const float yf = xh.y + uh.y;
     if (c.kind == CONTACT_SUBSTRATE) {
-        if (ws.wf - yf < -1e-3f) return 0.0;
+        if (ws.wf - yf < -1e-3f) return false;
         const float4 xl = *xlp;
         const double y = ((double)xh.y + (double)xl.y) + ((double)uh.y + (double)ul.y);
-        const double dis = fmax(w - y, 0.0);
-        const double fy = c.k * dis;
+        fy = c.k * fmax(w - y, 0.0);
         f.y += (float)fy;
-        return fy;
+        return true;
     }
     if (c.kind == CONTACT_PLANE) {
-        if (yf - ws.wf < -1e-3f) return 0.0;
+        if (yf - ws.wf < -1e-3f) return false;
         const float4 xl = *xlp;
         const double y = ((double)xh.y + (double)xl.y) + ((double)uh.y + (double)ul.y);
-        const double dis = fmax(y - w, 0.0);
-        const double fy = -c.k * dis;
+        fy = -c.k * fmax(y - w, 0.0);
         f.y += (float)fy;
-        return fy;
+        return true;
     }
     // sphere centred at (0, w, 0)
     const float rxf = xh.x + uh.x, ryf = yf - ws.wf, rzf = xh.z + uh.z;
     const float rr = ws.rf + 1e-3f;
-    if (rxf * rxf + ryf * ryf + rzf * rzf > rr * rr) return 0.0;
+    if (rxf * rxf + ryf * ryf + rzf * rzf > rr * rr) return false;
     const float4 xl = *xlp;
     const double rx = ((double)xh.x + (double)xl.x) + ((double)uh.x + (double)ul.x);
     const double ry = (((double)xh.y + (double)xl.y) + ((double)uh.y + (double)ul.y)) - w;
     const double rz = ((double)xh.z + (double)xl.z) + ((double)uh.z + (double)ul.z);
     const double len = sqrt(rx * rx + ry * ry + rz * rz);
     const double dis = fmax(c.radius - len, 0.0);
-    if (dis == 0.0) return 0.0;
+    if (dis == 0.0) return false;
     const double kd = c.k * dis;
-    const double fx = kd * (rx / len), fy = kd * (ry / len), fz = kd * (rz / len);
+    const double fx = kd * (rx / len), fz = kd * (rz / len);
+    fy = kd * (ry / len);
     f.x += (float)fx;
     f.y += (float)fy;
     f.z += (float)fz;
-    return fy;
+    return true;
 }
 
 // One node: element force from the fixed-point accumulator, the contacts in order (returns the
@@ -685,8 +744,8 @@ __device__ __forceinline__ double node_step(const MeshDev& m, const StateDev& s,
     float4 uh = s.uh[i], ul = s.ul[i];
     double ro = 0.0;
     for (int c = 0; c < nc; c++) {
-        const double fy = contact_force(cs[c], wall[c], xh, m.Xl + i, uh, ul, f);
-        if (c == rc) ro = -fy;
+        double fy;
+        if (contact_force(cs[c], wall[c], xh, m.Xl + i, uh, ul, f, fy) && c == rc) ro = -fy;
     }
     if (update && C.integrator == INTEGRATOR_VV2) {
         // velocityVerlet2.cl:9-13: v = (v + (a_old + f/m)/2) / (1 + xi/2); a = f/m - xi v;

@@ -152,28 +152,45 @@ bool build_mesh_plan(int64_t np, int64_t nt, const double* P, const uint32_t* T,
         slot_user.resize(s0 + T_, -1);
         plan.lconn.resize(4 * (s0 + T_), 0);
         plan.tile_inc.resize(4 * (s0 + T_), 0);
+        // Local node order: by incidence count, largest first (ties by node index). The thread of
+        // local node q sums its corners in a loop, and a warp runs as many iterations as its
+        // largest count, so grouping similar counts into the same warp saves iterations.
+        std::vector<uint32_t> cnt_by_id(nn, 0);
+        for (int64_t j = 0; j < cnt; j++) {
+            const int64_t ut = order[t0 + j];
+            for (int k = 0; k < 4; k++) {
+                const uint32_t g = (uint32_t)plan.node_int[T[k * nt + ut]];
+                cnt_by_id[std::lower_bound(ids.begin(), ids.end(), g) - ids.begin()]++;
+            }
+        }
+        std::vector<uint32_t> by_count(nn), loc_of(nn);
+        std::iota(by_count.begin(), by_count.end(), 0u);
+        std::stable_sort(by_count.begin(), by_count.end(),
+                         [&](uint32_t a, uint32_t c) { return cnt_by_id[a] > cnt_by_id[c]; });
+        for (size_t q = 0; q < nn; q++) loc_of[by_count[q]] = (uint32_t)q;
         std::vector<uint32_t> count(nn, 0), first(nn, 0);
         for (int64_t j = 0; j < cnt; j++) {
             const int64_t ut = order[t0 + j];
             slot_user[s0 + j] = ut;
             for (int k = 0; k < 4; k++) {
                 const uint32_t g = (uint32_t)plan.node_int[T[k * nt + ut]];
-                const size_t loc = std::lower_bound(ids.begin(), ids.end(), g) - ids.begin();
+                const uint32_t loc = loc_of[std::lower_bound(ids.begin(), ids.end(), g) - ids.begin()];
                 plan.lconn[4 * (s0 + j) + k] = (uint8_t)loc;
                 count[loc]++;
             }
         }
-        // incidence list of the tile: corners grouped by local node, in (tet, corner) order
+        // incidence list of the tile: corners grouped by local node, in (tet, corner) order, each
+        // entry the corner's slot in the kernels' corner-major shared array (corner * T + tet)
         for (size_t q = 1; q < nn; q++) first[q] = first[q - 1] + count[q - 1];
         std::vector<uint32_t> fill(first);
         for (int64_t j = 0; j < cnt; j++)
             for (int k = 0; k < 4; k++) {
                 const uint8_t loc = plan.lconn[4 * (s0 + j) + k];
-                plan.tile_inc[4 * s0 + fill[loc]++] = (uint16_t)(4 * j + k);
+                plan.tile_inc[4 * s0 + fill[loc]++] = (uint16_t)(k * T_ + j);
             }
         plan.tile_nodes.resize(2 * (size_t)((b + 1) * NM_), 0u);
         for (size_t q = 0; q < nn; q++) {
-            plan.tile_nodes[2 * (b * NM_ + q)] = ids[q];
+            plan.tile_nodes[2 * (b * NM_ + q)] = ids[by_count[q]];
             plan.tile_nodes[2 * (b * NM_ + q) + 1] = (first[q] << 16) | count[q];
         }
         plan.tile_meta.push_back((uint32_t)cnt | ((uint32_t)nn << 16));
