@@ -5,10 +5,13 @@
 //  * nodes are sorted along a Morton (Z-order) curve of their reference positions, and tetrahedra
 //    along the Morton curve of their centroids, so a run of consecutive tetrahedra touches a
 //    compact set of nodes;
-//  * consecutive tetrahedra are grouped into tiles of at most tile_tets (128, 256 or 512)
-//    elements and min(tile_tets, 256) distinct nodes, each tetra's corners stored as 8-bit
-//    indices into its tile's node list, plus the tile's incidence list (corners grouped by
-//    node) for the fixed-order force sums;
+//  * tetrahedra are grouped into tiles of at most tile_tets (128, 256 or 512) elements and
+//    min(tile_tets, 256) distinct nodes by greedy region growing: a tile starts at the first
+//    unassigned tetra along the Morton curve and repeatedly takes the adjacent tetra that adds
+//    the fewest new nodes, so tiles are compact and share few nodes (every node entry of a tile
+//    costs a displacement gather and three accumulator atomics per step). Each tetra's corners
+//    are stored as 8-bit indices into its tile's node list, plus the tile's incidence list
+//    (corners grouped by node) for the fixed-order force sums;
 //  * Dm^-1 (inverse of the reference edge matrix [X1-X0, X2-X0, X3-X0]) and the signed
 //    reference volume V0 = det(Dm)/6 (TetraCell.py:33-41) are computed in double and stored
 //    as float;
@@ -48,6 +51,91 @@ struct Quant {
         return (uint64_t)s;
     }
 };
+
+// Greedy region-growing tiles (see the file comment). seed_order: the tetrahedra in Morton
+// order. Appends each tile's tetrahedra to tets and the tiles' end offsets to tile_end.
+// Candidates are kept in five FIFO buckets by the number of nodes they would add (0..4); a
+// bucket entry is stale when the tetra was assigned or its count dropped since it was pushed.
+void grow_tiles(int64_t np, int64_t nt, const uint32_t* T, const std::vector<int64_t>& seed_order, int tile_tets,
+                int nodes_max, std::vector<uint32_t>& tets, std::vector<int64_t>& tile_end) {
+    std::vector<int64_t> off((size_t)np + 1, 0);  // node -> incident tetrahedra (CSR)
+    for (int64_t i = 0; i < 4 * nt; i++) off[(size_t)T[i] + 1]++;
+    for (int64_t i = 0; i < np; i++) off[i + 1] += off[i];
+    std::vector<uint32_t> adj((size_t)(4 * nt));
+    {
+        std::vector<int64_t> fill(off.begin(), off.end() - 1);
+        for (int64_t k = 0; k < 4; k++)
+            for (int64_t t = 0; t < nt; t++) adj[fill[T[k * nt + t]]++] = (uint32_t)t;
+    }
+    std::vector<uint8_t> assigned((size_t)nt, 0), newc((size_t)nt, 0);
+    std::vector<int64_t> node_stamp((size_t)np, -1), tet_stamp((size_t)nt, -1);
+    std::vector<uint32_t> bucket[5];
+    size_t head[5];
+    tets.clear();
+    tets.reserve((size_t)nt);
+    tile_end.clear();
+    int64_t seed = 0, tile = 0;
+    for (;;) {
+        while (seed < nt && assigned[seed_order[seed]]) seed++;
+        if (seed == nt) break;
+        for (int b = 0; b < 5; b++) {
+            bucket[b].clear();
+            head[b] = 0;
+        }
+        int nodes = 0, cnt = 0;
+        auto new_nodes = [&](uint32_t t) {
+            int c = 0;
+            for (int k = 0; k < 4; k++) c += node_stamp[T[k * nt + t]] != tile;
+            return c;
+        };
+        auto add = [&](uint32_t t) {
+            assigned[t] = 1;
+            tets.push_back(t);
+            cnt++;
+            for (int k = 0; k < 4; k++) {
+                const uint32_t n = T[k * nt + t];
+                if (node_stamp[n] == tile) continue;
+                node_stamp[n] = tile;
+                nodes++;
+                for (int64_t a = off[n]; a < off[n + 1]; a++) {
+                    const uint32_t t2 = adj[a];
+                    if (assigned[t2]) continue;
+                    if (tet_stamp[t2] != tile) {
+                        tet_stamp[t2] = tile;
+                        newc[t2] = (uint8_t)new_nodes(t2);
+                    } else if (newc[t2] > 0) {
+                        newc[t2]--;
+                    }
+                    bucket[newc[t2]].push_back(t2);
+                }
+            }
+        };
+        add((uint32_t)seed_order[seed]);
+        while (cnt < tile_tets) {
+            int64_t pick = -1;
+            for (int b = 0; b < 5 && pick < 0; b++) {
+                if (nodes + b > nodes_max) break;
+                while (head[b] < bucket[b].size()) {
+                    const uint32_t t = bucket[b][head[b]++];
+                    if (!assigned[t] && tet_stamp[t] == tile && newc[t] == b) {
+                        pick = t;
+                        break;
+                    }
+                }
+            }
+            if (pick < 0) {  // nothing adjacent fits: the next unassigned tetra along the curve
+                while (seed < nt && assigned[seed_order[seed]]) seed++;
+                if (seed == nt) break;
+                const uint32_t t = (uint32_t)seed_order[seed];
+                if (nodes + new_nodes(t) > nodes_max) break;
+                pick = t;
+            }
+            add((uint32_t)pick);
+        }
+        tile_end.push_back((int64_t)tets.size());
+        tile++;
+    }
+}
 
 }  // namespace
 
@@ -130,23 +218,23 @@ bool build_mesh_plan(int64_t np, int64_t nt, const double* P, const uint32_t* T,
     // Dm^-1 = 0 and V0 = 0 and produces no force; a padding node entry has count 0). Kernels can
     // then address a tile's data without first loading its offsets.
     const int64_t T_ = tile_tets, NM_ = nodes_max;
+    std::vector<uint32_t> tile_tets_list;
+    std::vector<int64_t> tile_end;
+    grow_tiles(np, nt, T, order, tile_tets, (int)nodes_max, tile_tets_list, tile_end);
+    order.assign(tile_tets_list.begin(), tile_tets_list.end());  // tetrahedra in tile order
     std::vector<int64_t> slot_user;  // tetra slot -> user tetra (-1: padding)
     std::vector<uint32_t> ids;
     ids.reserve(4 * (size_t)tile_tets);
     int64_t t0 = 0, b = 0;
     while (t0 < nt) {
-        int64_t cnt = std::min<int64_t>(tile_tets, nt - t0);
-        for (;;) {
-            ids.clear();
-            for (int64_t j = 0; j < cnt; j++) {
-                const int64_t ut = order[t0 + j];
-                for (int k = 0; k < 4; k++) ids.push_back((uint32_t)plan.node_int[T[k * nt + ut]]);
-            }
-            std::sort(ids.begin(), ids.end());
-            ids.erase(std::unique(ids.begin(), ids.end()), ids.end());
-            if ((int64_t)ids.size() <= nodes_max || cnt == 1) break;
-            cnt = std::max<int64_t>(1, cnt - 16);
+        const int64_t cnt = tile_end[b] - t0;
+        ids.clear();
+        for (int64_t j = 0; j < cnt; j++) {
+            const int64_t ut = order[t0 + j];
+            for (int k = 0; k < 4; k++) ids.push_back((uint32_t)plan.node_int[T[k * nt + ut]]);
         }
+        std::sort(ids.begin(), ids.end());
+        ids.erase(std::unique(ids.begin(), ids.end()), ids.end());
         const size_t nn = ids.size();
         const size_t s0 = (size_t)(b * T_);
         slot_user.resize(s0 + T_, -1);
