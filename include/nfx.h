@@ -185,6 +185,11 @@ int nfx_profile_steps(nfx_sim* sim, int64_t nsteps, float* tet_ms, float* node_m
  * undone before return. A timing helper with no counterpart in the reference. */
 int nfx_profile_tet_pass(nfx_sim* sim, int launches, float* ms);
 
+/* q[i] = a[i] / b[i] (host arrays of n floats) computed on `device` with the divide the element
+ * laws use, so a test can check its accuracy against correctly rounded division. A self-check
+ * with no counterpart in the reference. */
+int nfx_divide_check(int device, int64_t n, const float* a, const float* b, float* q);
+
 /* Number of mesh tiles and distinct-node entries (diagnostics for the tile layout). */
 int nfx_mesh_info(nfx_sim* sim, int64_t* ntiles, int64_t* tile_nodes);
 

@@ -886,6 +886,25 @@ int nfx_profile_tet_pass(nfx_sim* s, int launches, float* ms) {
     return NFX_OK;
 }
 
+int nfx_divide_check(int device, int64_t n, const float* a, const float* b, float* q) {
+    CHECK_ARG(a && b && q, "null argument");
+    CHECK_ARG(n >= 0 && n <= (int64_t)1 << 26, "n out of range [0, 2^26]");
+    if (n == 0) return NFX_OK;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return fail(NFX_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+    float* d = nullptr;
+    const size_t bytes = (size_t)n * sizeof(float);
+    e = cudaMalloc(&d, 3 * bytes);
+    if (e != cudaSuccess) return fail(NFX_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    e = cudaMemcpy(d, a, bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d + n, b, bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = launch_divide_check(d, d + n, d + 2 * n, (long long)n, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(q, d + 2 * n, bytes, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(NFX_ERR_CUDA, std::string("divide_check: ") + cudaGetErrorString(e));
+    return NFX_OK;
+}
+
 int nfx_mesh_info(nfx_sim* s, int64_t* ntiles, int64_t* tile_nodes) {
     CHECK_ARG(s && ntiles && tile_nodes, "null argument");
     if (!s->have_mesh) return fail(NFX_ERR_STATE, "no mesh");

@@ -201,6 +201,8 @@ cudaError_t launch_advance_time(const StateDev& s, long long n, long long fields
 // the current positions, for readouts between steps.
 cudaError_t launch_si_pass(const MeshDev& m, const StateDev& s, const BatchDev& b, int t_offset, bool readout,
                            int contact, cudaStream_t stream);
+// q[i] = a[i] / b[i] with the element laws' device divide (self-check of its accuracy).
+cudaError_t launch_divide_check(const float* a, const float* b, float* q, long long n, cudaStream_t stream);
 // Conversions between the user's layout (SoA doubles, user order) and the device state.
 cudaError_t launch_points_to_user(const MeshDev& m, const StateDev& s, const long long* node_user, double* out,
                                   cudaStream_t stream);

@@ -683,50 +683,65 @@ struct WallStep {
     float wf, rf;
 };
 
-// Contact force on one node in double precision (the reference's FP64 formulas). Returns false
-// for a node out of contact (no force); otherwise adds the force to f and returns its y component
-// in fy for the readout. Only nodes that pass the coarse float test read the low part of the
-// reference position or do any double arithmetic (the FP64 pipe is narrow on this GPU).
+// The exact contact force (the reference's FP64 formulas) on one node that passed the coarse
+// float test. Every double term is formed after the low-part load, so none of the double
+// arithmetic can be hoisted above the coarse test: with the terms of (x_hi + x_lo) + (u_hi + u_lo)
+// independent of that load, the compiler ran the displacement sums for every node (about three
+// DADDs per node on the narrow FP64 pipe). hit = false: the node does not touch (sphere only).
+struct ContactForce {
+    double fx, fy, fz;
+    bool hit;
+};
+__device__ __forceinline__ ContactForce contact_exact(const ContactDev& c, double w, float4 xh, float4 xl, float4 uh,
+                                                      float4 ul) {
+    ContactForce r{0.0, 0.0, 0.0, true};
+    const double y = (((double)xh.y + (double)xl.y) + (double)uh.y) + (double)ul.y;
+    if (c.kind == CONTACT_SUBSTRATE || c.kind == CONTACT_PLANE) {
+        r.fy = c.kind == CONTACT_SUBSTRATE ? c.k * fmax(w - y, 0.0) : -c.k * fmax(y - w, 0.0);
+        return r;
+    }
+    // sphere centred at (0, w, 0)
+    const double rx = (((double)xh.x + (double)xl.x) + (double)uh.x) + (double)ul.x;
+    const double ry = y - w;
+    const double rz = (((double)xh.z + (double)xl.z) + (double)uh.z) + (double)ul.z;
+    const double len = sqrt(rx * rx + ry * ry + rz * rz);
+    const double dis = fmax(c.radius - len, 0.0);
+    if (dis == 0.0) {
+        r.hit = false;
+        return r;
+    }
+    const double kd = c.k * dis;
+    r.fx = kd * (rx / len);
+    r.fy = kd * (ry / len);
+    r.fz = kd * (rz / len);
+    return r;
+}
+
+// Contact force on one node: the coarse test in float (nodes farther than 1e-3 from contact
+// cannot touch), then the exact force. Returns false for a node out of contact; otherwise adds
+// the force to f and returns its y component in fy for the readout.
 __device__ __forceinline__ bool contact_force(const ContactDev& c, const WallStep& ws, const float4& xh,
                                               const float4* xlp, const float4& uh, const float4& ul, float4& f,
                                               double& fy) {
     if (c.kind == CONTACT_SPHERE_INTEGRAL) return false;  // a per-tetra force (element pass)
-    const double w = ws.w;
-    // coarse test in float: nodes farther than 1e-3 from contact cannot touch
     const float yf = xh.y + uh.y;
     if (c.kind == CONTACT_SUBSTRATE) {
         if (ws.wf - yf < -1e-3f) return false;
-        const float4 xl = *xlp;
-        const double y = ((double)xh.y + (double)xl.y) + ((double)uh.y + (double)ul.y);
-        fy = c.k * fmax(w - y, 0.0);
-        f.y += (float)fy;
-        return true;
-    }
-    if (c.kind == CONTACT_PLANE) {
+    } else if (c.kind == CONTACT_PLANE) {
         if (yf - ws.wf < -1e-3f) return false;
-        const float4 xl = *xlp;
-        const double y = ((double)xh.y + (double)xl.y) + ((double)uh.y + (double)ul.y);
-        fy = -c.k * fmax(y - w, 0.0);
-        f.y += (float)fy;
-        return true;
+    } else {
+        const float rxf = xh.x + uh.x, ryf = yf - ws.wf, rzf = xh.z + uh.z;
+        const float rr = ws.rf + 1e-3f;
+        if (rxf * rxf + ryf * ryf + rzf * rzf > rr * rr) return false;
     }
-    // sphere centred at (0, w, 0)
-    const float rxf = xh.x + uh.x, ryf = yf - ws.wf, rzf = xh.z + uh.z;
-    const float rr = ws.rf + 1e-3f;
-    if (rxf * rxf + ryf * ryf + rzf * rzf > rr * rr) return false;
-    const float4 xl = *xlp;
-    const double rx = ((double)xh.x + (double)xl.x) + ((double)uh.x + (double)ul.x);
-    const double ry = (((double)xh.y + (double)xl.y) + ((double)uh.y + (double)ul.y)) - w;
-    const double rz = ((double)xh.z + (double)xl.z) + ((double)uh.z + (double)ul.z);
-    const double len = sqrt(rx * rx + ry * ry + rz * rz);
-    const double dis = fmax(c.radius - len, 0.0);
-    if (dis == 0.0) return false;
-    const double kd = c.k * dis;
-    const double fx = kd * (rx / len), fz = kd * (rz / len);
-    fy = kd * (ry / len);
-    f.x += (float)fx;
-    f.y += (float)fy;
-    f.z += (float)fz;
+    const ContactForce r = contact_exact(c, ws.w, xh, *xlp, uh, ul);
+    if (!r.hit) return false;
+    if (c.kind == CONTACT_SPHERE) {
+        f.x += (float)r.fx;
+        f.z += (float)r.fz;
+    }
+    f.y += (float)r.fy;
+    fy = r.fy;
     return true;
 }
 
@@ -1069,6 +1084,17 @@ cudaError_t launch_advance_time(const StateDev& s, long long n, long long fields
 cudaError_t launch_points_to_user(const MeshDev& m, const StateDev& s, const long long* node_user, double* out,
                                   cudaStream_t st) {
     k_points_to_user<<<(m.np + 255) / 256, 256, 0, st>>>(m, s, node_user, out);
+    return cudaGetLastError();
+}
+
+__global__ void k_divide_check(const float* a, const float* b, float* q, long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) q[i] = fdiv_(a[i], b[i]);
+}
+
+cudaError_t launch_divide_check(const float* a, const float* b, float* q, long long n, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_divide_check<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a, b, q, n);
     return cudaGetLastError();
 }
 

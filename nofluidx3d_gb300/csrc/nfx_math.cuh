@@ -33,11 +33,27 @@ NFX_HD float rcbrt_(float x) {
 }
 NFX_HD float pow_(float x, float y) { return powf(x, y); }
 NFX_HD float sqrt_(float x) { return sqrtf(x); }
-// a / b to within 2 ulp (the reciprocal-based divide), used where FP32 rounding of the quotient
-// is far below the scheme's other errors.
+// a / b for the element laws. The fast reciprocal-based divide (__fdividef, up to 2 ulp) is
+// refined by Markstein's method (P. Markstein, "IA-64 and Elementary Functions", 2000): one
+// Newton-Raphson step on the reciprocal, r' = r + r (1 - b r), then the quotient corrected by its
+// exact residual, q' = q + r' (a - b q), each residual a single fused multiply-add. Four FMAs and
+// no branch; the result agrees with the correctly rounded quotient to within 1 ulp (checked
+// against a / b on the GPU in the tests). The plastic state integrates quotients over every step,
+// and the fast divide's bias alone moved the 10^4-step viscoplastic force curve by 1e-5.
+// Valid for normal |b| below 2^126 (the element laws divide by determinants and stresses).
+#ifndef NFX_DIV_REFINE
+#define NFX_DIV_REFINE 1  // 0: the fast divide alone
+#endif
 NFX_HD float fdiv_(float a, float b) {
 #if defined(__CUDA_ARCH__)
-    return __fdividef(a, b);
+    float r = __fdividef(1.0f, b);
+#if NFX_DIV_REFINE
+    r = fmaf(r, fmaf(-b, r, 1.0f), r);
+    const float q = a * r;
+    return fmaf(r, fmaf(-b, q, a), q);
+#else
+    return a * r;
+#endif
 #else
     return a / b;
 #endif

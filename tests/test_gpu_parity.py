@@ -200,9 +200,9 @@ def test_sphere_integral_readout_in_step_equals_on_demand():
 
 def test_gpu_viscoplastic_sphere_10k_steps_vs_fp64_oracle():
     """R=8 Mooney-Rivlin + viscoplastic cell under a sphere of radius 2, 10^4 steps, against the
-    FP64 oracle. Measured on GB300: trajectory 1.4e-6 (bar 1e-5), curve 2.9e-4 L2 — three times
-    the 1e-4 bar, where a direct FP32 port of the reference reaches 1.8e-5 and 1.4e-2. The
-    bounds below guard that level."""
+    FP64 oracle, at the bars of 1e-5 (trajectories) and 1e-4 (force curve). Measured on GB300:
+    trajectory 4.7e-7, curve 9.3e-5 L2, where a direct FP32 port of the reference reaches 1.8e-5
+    and 1.4e-2 (and the same kernels with the unrefined fast divide 1.03e-4)."""
     from nofluidx3d_gb300.workloads import plain_large
 
     w = plain_large().with_(name="R8 VP sphere", radius=8.0, sphere_radius=2.0, speed=1e-4, record_every=100)
@@ -216,5 +216,5 @@ def test_gpu_viscoplastic_sphere_10k_steps_vs_fp64_oracle():
     sim.record_now()
     assert sim.status() == 0
     assert rel_traj(st.positions(), sim.points()) < TRAJ_TOL
-    assert rel_curve(cref, sim.curve()) < 1e-3
+    assert rel_curve(cref, sim.curve()) < CURVE_TOL
     sim.close()
