@@ -61,18 +61,40 @@ def load_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def load_traffic(workload_key: str) -> float | None:
-    """DRAM bytes per tetra of the element pass from the committed ncu summary, if any."""
+def profile_figure(workload_key: str, name: str) -> float | None:
+    """A per-tetra figure of the element pass (a "name: value" line) from the committed ncu
+    summary of the workload, if any."""
     p = os.path.join(ROOT, "profiles", f"tet_pass_{workload_key}.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
-        if line.startswith("dram_bytes_per_tetra:"):
+        if line.startswith(name + ":"):
             try:
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
                 return None
     return None
+
+
+def load_traffic(workload_key: str) -> float | None:
+    """DRAM bytes per tetra of the element pass from the committed ncu summary, if any."""
+    return profile_figure(workload_key, "dram_bytes_per_tetra")
+
+
+def fp32_rate(flops_per_tet: float | None, nt: int, tet_ms: float, device: int, clk: dict) -> dict | None:
+    """Achieved FP32 rate of the element pass: ncu-counted FP32 FLOPs per tetra (2 per FFMA, 1 per
+    FADD/FMUL) x tetra / its average launch time, against the nominal FMA peak of the device
+    (SMs x 128 FP32 lanes x 2 FLOP x maximum SM clock)."""
+    if flops_per_tet is None:
+        return None
+    import torch
+
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    mhz = (clk or {}).get("sm_max_mhz") or 2070.0
+    peak = sms * 128 * 2 * mhz * 1e6 / 1e12
+    achieved = flops_per_tet * nt / (tet_ms / 1e3) / 1e12
+    return {"flops_per_tetra": flops_per_tet, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "peak_source": "nominal"}
 
 
 class ClockSampler:
@@ -351,6 +373,7 @@ def main():
     achieved = elem_bytes / (tet_launch_ms / 1e3) / 1e9
     peaks = load_peaks()
     traffic_per_tet = load_traffic(args.workload)
+    flops_per_tet = profile_figure(args.workload, "fp32_flops_per_tetra")
 
     # end to end through the C ABI with pinned host buffers
     import torch
@@ -404,6 +427,7 @@ def main():
                      "kernel": "k_tet_pass (element pass)", "launches_timed": args.tet_launches,
                      "algorithmic_bytes_per_launch": elem_bytes,
                      "traffic": None if traffic_per_tet is None else traffic_per_tet * nt},
+        "fp32": fp32_rate(flops_per_tet, nt, tet_launch_ms, local, clk),
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_val, "unit": "tetra-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": 2 * args.steps + (args.steps + 99) // 100,

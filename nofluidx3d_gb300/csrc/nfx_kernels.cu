@@ -746,7 +746,8 @@ __device__ __forceinline__ bool contact_force(const ContactDev& c, const WallSte
 }
 
 // One node: element force from the fixed-point accumulator, the contacts in order (returns the
-// readout value -f_y of contact rc), and in update mode the cell's integrator with the
+// y force of contact rc on the node; the readout is minus its sum, negated once per cell so that
+// no node runs a double negation), and in update mode the cell's integrator with the
 // displacement carried as hi + lo — damped velocity Verlet with unit mass and the FIXED_TOP_BOTTOM
 // pin (VelocityVerlet.cl), or the lumped-mass form (velocityVerlet2.cl) — and the accumulator reset.
 __device__ __forceinline__ double node_step(const MeshDev& m, const StateDev& s, int i, const WallStep* wall,
@@ -757,10 +758,10 @@ __device__ __forceinline__ double node_step(const MeshDev& m, const StateDev& s,
     float4 f = make_float4(fix_to_float(s.facc[i]), fix_to_float(s.facc[np + i]), fix_to_float(s.facc[2 * np + i]), 0.f);
     const float4 xh = m.Xh[i];
     float4 uh = s.uh[i], ul = s.ul[i];
-    double ro = 0.0;
+    double fy_rc = 0.0;
     for (int c = 0; c < nc; c++) {
         double fy;
-        if (contact_force(cs[c], wall[c], xh, m.Xl + i, uh, ul, f, fy) && c == rc) ro = -fy;
+        if (contact_force(cs[c], wall[c], xh, m.Xl + i, uh, ul, f, fy) && c == rc) fy_rc = fy;
     }
     if (update && C.integrator == INTEGRATOR_VV2) {
         // velocityVerlet2.cl:9-13: v = (v + (a_old + f/m)/2) / (1 + xi/2); a = f/m - xi v;
@@ -811,7 +812,7 @@ __device__ __forceinline__ double node_step(const MeshDev& m, const StateDev& s,
         s.facc[np + i] = 0ull;
         s.facc[2 * np + i] = 0ull;
     }
-    return ro;
+    return fy_rc;
 }
 
 // One thread per node. The block's cell (cell 0 without a block map) supplies the contacts and
@@ -855,13 +856,13 @@ __global__ void __launch_bounds__(NODE_BLOCK, NFX_NODE_MIN_BLOCKS) k_node_pass(M
             }
         }
     }
-    double ro = 0.0;
+    double fy = 0.0;  // y force of the readout contact on this node
     if (i < C.node_end)
-        ro = node_step(m, s, i, s_wall, C, rc, mode == NODE_UPDATE, bd.cell_status ? bd.cell_status + cell : nullptr);
+        fy = node_step(m, s, i, s_wall, C, rc, mode == NODE_UPDATE, bd.cell_status ? bd.cell_status + cell : nullptr);
     if (!rec) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    ro = warp_sum_d(ro);
-    if (lane == 0) s_w[warp] = ro;
+    fy = warp_sum_d(fy);
+    if (lane == 0) s_w[warp] = fy;
     __syncthreads();
     if (warp == 0) {
         double x = lane < NODE_BLOCK / 32 ? s_w[lane] : 0.0;
@@ -880,17 +881,20 @@ __global__ void __launch_bounds__(NODE_BLOCK, NFX_NODE_MIN_BLOCKS) k_node_pass(M
     double acc = 0.0;
     for (int k = C.block_begin + threadIdx.x; k < C.block_end; k += NODE_BLOCK) acc += part[k];
     if (rc >= 0 && rc == C.si_contact) {
-        // integrated sphere: -sum of the y forces, summed per tile by the element pass (or by
-        // k_si_partials for an on-demand readout)
+        // integrated sphere: the y forces summed per tile by the element pass (or by the sphere
+        // pass for an on-demand readout)
         const volatile double* tp = s.tile_partials;
-        for (int k = C.tile_begin + threadIdx.x; k < C.tile_end; k += NODE_BLOCK) acc -= tp[k];
+        for (int k = C.tile_begin + threadIdx.x; k < C.tile_end; k += NODE_BLOCK) acc += tp[k];
     }
     acc = warp_sum_d(acc);
     if (lane == 0) s_w[warp] = acc;
     __syncthreads();
     if (threadIdx.x == 0) {
-        double tot = 0.0;
-        for (int w = 0; w < NODE_BLOCK / 32; w++) tot += s_w[w];
+        double sum = 0.0;
+        for (int w = 0; w < NODE_BLOCK / 32; w++) sum += s_w[w];
+        // the readout is minus the summed y force (negation is exact and rounding is symmetric,
+        // so this equals summing the negated forces)
+        const double tot = 0.0 - sum;
         if (mode == NODE_READOUT_VALUE) {
             s.force_out[cell] = tot;
         } else {
