@@ -74,10 +74,7 @@ struct nfx_sim {
     long long time = 0;          // host mirror of the device time
     cudaGraphExec_t graph = nullptr;
     bool graph_valid = false;
-    int sm_count = 1;
-    int tet_variant = 0;                   // 1: persistent pipelined element pass, 0: one CTA per tile
     int tile_tets = DEFAULT_TILE_TETS;     // tetrahedra per tile (64, 128, 256 or 512)
-    int pipe_bps[4] = {-1, -1, -1, -1};    // resident CTAs per SM of the pipelined kernel, per model
 };
 
 namespace {
@@ -145,19 +142,8 @@ int upload_cell(nfx_sim* s) {
     return NFX_OK;
 }
 
-// Element pass launch: the one-CTA-per-tile kernel by default. NFX_TET_KERNEL=1 in the
-// environment selects the persistent pipelined kernel (tiles of at most 256) on a grid of
-// (resident CTAs per SM) x (SM count), capped at the tile count.
+// Element pass launch: one CTA per tile.
 cudaError_t launch_elem(nfx_sim* s, int k) {
-    if (s->tet_variant == 1 && s->mesh.tile_tets <= TILE_TETS) {
-        const int model = s->cell.mat.model;
-        int& bps = s->pipe_bps[model & 3];
-        if (bps < 0) bps = pipe_blocks_per_sm(model, s->mesh.tile_tets);
-        if (bps > 0) {
-            const long long grid = std::min<long long>((long long)bps * s->sm_count, s->mesh.ntiles);
-            return launch_tet_pass_pipe(s->mesh, s->st, table_view(s), model, k, (int)grid, s->stream);
-        }
-    }
     return launch_tet_pass(s->mesh, s->st, table_view(s), s->cell.mat.model, k, s->stream);
 }
 
@@ -266,9 +252,6 @@ int nfx_create(int device, nfx_sim** out) {
     s->cell.fix_a = s->cell.fix_b = -1;
     s->cell.si_contact = -1;
     s->cell.integrator = INTEGRATOR_VV;
-    cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, device);
-    if (s->sm_count < 1) s->sm_count = 1;
-    if (const char* v = std::getenv("NFX_TET_KERNEL")) s->tet_variant = std::atoi(v) == 1 ? 1 : 0;
     if (const char* v = std::getenv("NFX_TILE_TETS")) {
         const int t = std::atoi(v);
         if (t == 64 || t == 128 || t == 256 || t == 512) s->tile_tets = t;

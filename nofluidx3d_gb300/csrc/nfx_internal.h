@@ -17,7 +17,6 @@ constexpr int MAX_CONTACTS = 4;
 // A tile is a run of consecutive tetrahedra (after reordering) processed by one CTA. Its
 // distinct nodes are listed once, so the per-tetra connectivity is four 8-bit local indices
 // and the tile's nodal forces are summed in shared memory before one flush per node.
-constexpr int TILE_TETS = 256;          // largest tile of the pipelined kernel
 constexpr int DEFAULT_TILE_TETS = 128;  // fastest measured on GB300 (R=64 viscoplastic cell)
 constexpr int TILE_NODES_MAX = 256;  // 8-bit local corner indices
 // Tile sizes the one-CTA-per-tile kernel is built for; a tile has at most min(tile, 256) nodes.
@@ -182,11 +181,6 @@ void set_error(const std::string& msg);
 // Element pass over all tiles (one CTA per tile), material from the cell table.
 cudaError_t launch_tet_pass(const MeshDev& m, const StateDev& s, const BatchDev& b, int model, int t_offset,
                             cudaStream_t stream);
-// Persistent, bulk-copy-pipelined element pass of a one-cell table: `grid` CTAs walk all tiles.
-cudaError_t launch_tet_pass_pipe(const MeshDev& m, const StateDev& s, const BatchDev& b, int model, int t_offset,
-                                 int grid, cudaStream_t stream);
-// Resident CTAs per SM of the pipelined element pass for a material model and tile size.
-int pipe_blocks_per_sm(int model, int tile);
 enum NodeMode : int { NODE_UPDATE = 0, NODE_READOUT_ROW = 1, NODE_READOUT_VALUE = 2 };
 // Node pass over `nblocks` node blocks. NODE_READOUT_VALUE sums contact `readout_contact`'s force
 // per cell into force_out[cell] without updating the state.

@@ -437,236 +437,6 @@ __global__ void __launch_bounds__(TILE) k_si_pass(MeshDev m, StateDev s, BatchDe
 }
 
 // ------------------------------------------------------------------------------------------
-// Element pass, persistent and pipelined
-//
-// Each CTA walks the tiles blockIdx.x, blockIdx.x + gridDim.x, ... through two shared-memory
-// stages. One thread fills a stage with the tile's contiguous per-tetra streams and node list by
-// bulk asynchronous copies (cp.async.bulk, the TMA engine) that complete on the stage's
-// mbarrier; one tile ahead, all threads gather the tile's node displacements with cp.async.
-// While tile i is evaluated, tile i+1's node data and tile i+2's streams are in flight.
-// ------------------------------------------------------------------------------------------
-template <int TILE>
-struct StageLayout {
-    static constexpr int NMAX = TILE < TILE_NODES_MAX ? TILE : TILE_NODES_MAX;  // nodes per tile
-    // byte offsets inside one stage (all multiples of 16)
-    static constexpr unsigned LCONN = 0;                  // uchar4[TILE]
-    static constexpr unsigned DMI_A = LCONN + 4 * TILE;   // float4[TILE]
-    static constexpr unsigned DMI_B = DMI_A + 16 * TILE;  // float4[TILE]
-    static constexpr unsigned DMI_C = DMI_B + 16 * TILE;  // float2[TILE]
-    static constexpr unsigned INC = DMI_C + 8 * TILE;     // ushort4[TILE]
-    static constexpr unsigned NODES = INC + 8 * TILE;     // uint2[NMAX + 2]
-    static constexpr unsigned UH = NODES + 8 * (NMAX + 2);
-    static constexpr unsigned UL = UH + 16 * NMAX;
-    static constexpr unsigned VP_A = UL + 16 * NMAX;
-    static constexpr unsigned VP_B = VP_A + 16 * TILE;
-    static constexpr unsigned VP_C = VP_B + 16 * TILE;
-    static constexpr unsigned SIZE_ELASTIC = VP_A;
-    static constexpr unsigned SIZE_VP = VP_C + 8 * TILE;
-    static_assert(UH % 16 == 0 && SIZE_VP % 16 == 0, "stage layout must be 16-byte aligned");
-};
-
-constexpr unsigned PIPE_HDR_BYTES = 64;  // two mbarriers + two stage headers
-
-template <int TILE>
-__host__ __device__ constexpr unsigned pipe_stage_bytes(int model) {
-    return model == MODEL_VP ? StageLayout<TILE>::SIZE_VP : StageLayout<TILE>::SIZE_ELASTIC;
-}
-template <int TILE>
-__host__ __device__ constexpr unsigned pipe_smem_bytes(int model) {
-    return 2 * pipe_stage_bytes<TILE>(model) + 16u * 4u * TILE + PIPE_HDR_BYTES;
-}
-
-__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
-    unsigned ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// Bounded wait: gives up after MBAR_WAIT_LIMIT polls (each try_wait may itself suspend briefly).
-constexpr int MBAR_WAIT_LIMIT = 1 << 22;
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
-    for (int i = 0; i < MBAR_WAIT_LIMIT; i++)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
-}
-__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_addr(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
-__device__ __forceinline__ unsigned round16(unsigned b) { return (b + 15u) & ~15u; }
-
-struct StageHdr {
-    int tb, ntt, nn, noff;
-};
-
-// Thread 0: issue the bulk copies of `tile` into stage `st` (header written first; the
-// mbarrier's release/acquire makes it visible to the waiting threads).
-template <int MODEL, int TILE>
-__device__ __forceinline__ void issue_tile(const MeshDev& m, const StateDev& s, int tile, unsigned char* st,
-                                           StageHdr* hdr, unsigned long long* bar) {
-    using StageLayout = nfx::StageLayout<TILE>;
-    // fixed-stride tiles: slots from tile*TILE, node entries from tile*NMAX (NMAX even, so the
-    // node list starts on a 16-byte boundary); real counts from the meta word
-    const unsigned meta = m.tile_meta[tile];
-    const int tb = tile * TILE, ntt = (int)(meta & 0xffffu);
-    const int nb = tile * StageLayout::NMAX, nn = (int)(meta >> 16);
-    const int nb0 = nb & ~1;
-    const int noff = nb - nb0;
-    const unsigned nodes_b = round16(8u * (unsigned)(nn + noff));
-    const unsigned b4 = round16(4u * ntt), b8 = round16(8u * ntt), b16 = 16u * ntt;
-    unsigned total = b4 + 2 * b16 + 2 * b8 + nodes_b;
-    if (MODEL == MODEL_VP) total += 2 * b16 + b8;
-    hdr->tb = tb;
-    hdr->ntt = ntt;
-    hdr->nn = nn;
-    hdr->noff = noff;
-    mbar_arrive_expect_tx(bar, total);
-    bulk_load(st + StageLayout::LCONN, m.lconn + tb, b4, bar);
-    bulk_load(st + StageLayout::DMI_A, m.dmi_a + tb, b16, bar);
-    bulk_load(st + StageLayout::DMI_B, m.dmi_b + tb, b16, bar);
-    bulk_load(st + StageLayout::DMI_C, m.dmi_c + tb, b8, bar);
-    bulk_load(st + StageLayout::INC, m.tile_inc + tb, b8, bar);
-    bulk_load(st + StageLayout::NODES, m.tile_nodes + nb0, nodes_b, bar);
-    if (MODEL == MODEL_VP) {
-        bulk_load(st + StageLayout::VP_A, s.vp_a + tb, b16, bar);
-        bulk_load(st + StageLayout::VP_B, s.vp_b + tb, b16, bar);
-        bulk_load(st + StageLayout::VP_C, s.vp_c + tb, b8, bar);
-    }
-}
-
-// All threads: gather the node displacements of the tile in stage `st` (cp.async, one group).
-template <int TILE>
-__device__ __forceinline__ void gather_nodes(const StateDev& s, unsigned char* st, const StageHdr& h) {
-    using StageLayout = nfx::StageLayout<TILE>;
-    const uint2* nodes = reinterpret_cast<const uint2*>(st + StageLayout::NODES) + h.noff;
-    float4* uh = reinterpret_cast<float4*>(st + StageLayout::UH);
-    float4* ul = reinterpret_cast<float4*>(st + StageLayout::UL);
-    for (int j = threadIdx.x; j < h.nn; j += TILE) {
-        const unsigned g = nodes[j].x;
-        cp_async16(uh + j, s.uh + g);
-        cp_async16(ul + j, s.ul + g);
-    }
-    cp_async_commit();
-}
-
-template <int MODEL, int TILE>
-__global__ void __launch_bounds__(TILE) k_tet_pass_pipe(MeshDev m, StateDev s, BatchDev bd, int t_offset) {
-    using StageLayout = nfx::StageLayout<TILE>;
-    extern __shared__ __align__(128) unsigned char smem[];
-    constexpr unsigned SB = pipe_stage_bytes<TILE>(MODEL);
-    constexpr unsigned PIPE_CF_BYTES = 16u * 4u * TILE;
-    unsigned char* stage[2] = {smem, smem + SB};
-    float4* s_cf = reinterpret_cast<float4*>(smem + 2 * SB);
-    unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem + 2 * SB + PIPE_CF_BYTES);
-    StageHdr* hdr = reinterpret_cast<StageHdr*>(smem + 2 * SB + PIPE_CF_BYTES + 16);
-    __shared__ int s_ok;
-
-    const int j = threadIdx.x;
-    const int G = gridDim.x;
-    const int first = blockIdx.x;
-    const bool wf = clock_bit(s.clock->fields_due, t_offset);
-    const MaterialDev mat = bd.cells[0].mat;
-    if (first >= m.ntiles) return;
-
-    if (j == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        issue_tile<MODEL, TILE>(m, s, first, stage[0], &hdr[0], &bar[0]);
-        if (first + G < m.ntiles) issue_tile<MODEL, TILE>(m, s, first + G, stage[1], &hdr[1], &bar[1]);
-        s_ok = mbar_wait_bounded(&bar[0], 0);
-    }
-    __syncthreads();
-    bool ok = s_ok != 0;
-    if (ok) gather_nodes<TILE>(s, stage[0], hdr[0]);
-
-    for (int it = 0; ok; it++) {
-        const int tile = first + it * G;
-        if (tile >= m.ntiles) break;
-        const int cur = it & 1, nxt = cur ^ 1;
-        const bool has_next = tile + G < m.ntiles;
-        // tile it+1: wait for its streams, start gathering its nodes
-        if (has_next) {
-            if (j == 0) s_ok = mbar_wait_bounded(&bar[nxt], (unsigned)((it + 1) >> 1) & 1u);
-            __syncthreads();
-            if (!s_ok) {
-                ok = false;
-                break;
-            }
-            gather_nodes<TILE>(s, stage[nxt], hdr[nxt]);
-            cp_async_wait<1>();
-        } else {
-            cp_async_wait<0>();
-        }
-        __syncthreads();  // tile it: streams and node data visible to all threads
-
-        const StageHdr h = hdr[cur];
-        unsigned char* st = stage[cur];
-        if (j < h.ntt) {
-            const float4* vpa = reinterpret_cast<const float4*>(st + StageLayout::VP_A);
-            const float4* vpb = reinterpret_cast<const float4*>(st + StageLayout::VP_B);
-            const float2* vpc = reinterpret_cast<const float2*>(st + StageLayout::VP_C);
-            float4 pa = make_float4(0.f, 0.f, 0.f, 0.f), pb = pa;
-            float2 pc = make_float2(0.f, 0.f);
-            if (MODEL == MODEL_VP) {
-                pa = vpa[j];
-                pb = vpb[j];
-                pc = vpc[j];
-            }
-            if (element_eval<MODEL, TILE>(j, (long long)h.tb + j, reinterpret_cast<const uchar4*>(st + StageLayout::LCONN)[j],
-                                reinterpret_cast<const float4*>(st + StageLayout::DMI_A)[j],
-                                reinterpret_cast<const float4*>(st + StageLayout::DMI_B)[j],
-                                reinterpret_cast<const float2*>(st + StageLayout::DMI_C)[j], pa, pb, pc,
-                                reinterpret_cast<const float4*>(st + StageLayout::UH),
-                                reinterpret_cast<const float4*>(st + StageLayout::UL), s_cf, s, mat, wf))
-                atomicOr(s.status, STATUS_INVERTED);
-        }
-        __syncthreads();  // corner forces complete
-        if (j < h.nn) {
-            const uint2 node = reinterpret_cast<const uint2*>(st + StageLayout::NODES)[h.noff + j];
-            if (!node_flush<TILE>(node, reinterpret_cast<const unsigned short*>(st + StageLayout::INC), s_cf, s, m.np))
-                atomicOr(s.status, STATUS_NONFINITE);
-        }
-        __syncthreads();  // stage `cur` and the corner forces are free again
-        if (j == 0 && tile + 2 * G < m.ntiles) {
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue_tile<MODEL, TILE>(m, s, tile + 2 * G, stage[cur], &hdr[cur], &bar[cur]);
-        }
-    }
-    cp_async_wait<0>();
-    if (!ok && j == 0) {
-        atomicOr(s.status, STATUS_TIMEOUT);
-        // let copies still in flight land before the CTA's shared memory is released
-        mbar_wait_bounded(&bar[0], 0);
-        mbar_wait_bounded(&bar[1], 0);
-    }
-}
-
-// ------------------------------------------------------------------------------------------
 // Node pass
 // ------------------------------------------------------------------------------------------
 __device__ __forceinline__ double warp_sum_d(double v) {
@@ -970,69 +740,6 @@ __global__ void k_vec_from_user(int np, float4* a, const long long* node_user, c
 // ------------------------------------------------------------------------------------------
 // Launchers
 // ------------------------------------------------------------------------------------------
-template <int MODEL, int TILE>
-static cudaError_t launch_pipe(const MeshDev& m, const StateDev& s, const BatchDev& b, int t_offset, int grid,
-                               cudaStream_t st) {
-    const unsigned bytes = pipe_smem_bytes<TILE>(MODEL);
-    static bool attr_set = false;  // per process; the attribute is per function
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_tet_pass_pipe<MODEL, TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)bytes);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
-    k_tet_pass_pipe<MODEL, TILE><<<grid, TILE, bytes, st>>>(m, s, b, t_offset);
-    return cudaGetLastError();
-}
-
-template <int TILE>
-static int pipe_bps_tile(int model) {
-    int n = 0;
-    cudaError_t e = cudaSuccess;
-    auto q = [&](auto kern, unsigned bytes) {
-        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, TILE, bytes);
-    };
-    switch (model) {
-        case MODEL_MR: q(k_tet_pass_pipe<MODEL_MR, TILE>, pipe_smem_bytes<TILE>(MODEL_MR)); break;
-        case MODEL_SVK: q(k_tet_pass_pipe<MODEL_SVK, TILE>, pipe_smem_bytes<TILE>(MODEL_SVK)); break;
-        case MODEL_SVKK: q(k_tet_pass_pipe<MODEL_SVKK, TILE>, pipe_smem_bytes<TILE>(MODEL_SVKK)); break;
-        default: q(k_tet_pass_pipe<MODEL_VP, TILE>, pipe_smem_bytes<TILE>(MODEL_VP)); break;
-    }
-    return e == cudaSuccess ? n : 0;
-}
-
-int pipe_blocks_per_sm(int model, int tile) {
-    switch (tile) {
-        case 64: return pipe_bps_tile<64>(model);
-        case 128: return pipe_bps_tile<128>(model);
-        case 256: return pipe_bps_tile<256>(model);
-        default: return 0;
-    }
-}
-
-template <int TILE>
-static cudaError_t launch_pipe_tile(const MeshDev& m, const StateDev& s, const BatchDev& b, int model, int t_offset,
-                                    int grid, cudaStream_t st) {
-    switch (model) {
-        case MODEL_MR: return launch_pipe<MODEL_MR, TILE>(m, s, b, t_offset, grid, st);
-        case MODEL_SVK: return launch_pipe<MODEL_SVK, TILE>(m, s, b, t_offset, grid, st);
-        case MODEL_SVKK: return launch_pipe<MODEL_SVKK, TILE>(m, s, b, t_offset, grid, st);
-        case MODEL_VP: return launch_pipe<MODEL_VP, TILE>(m, s, b, t_offset, grid, st);
-        default: return cudaErrorInvalidValue;
-    }
-}
-
-cudaError_t launch_tet_pass_pipe(const MeshDev& m, const StateDev& s, const BatchDev& b, int model, int t_offset,
-                                 int grid, cudaStream_t st) {
-    switch (m.tile_tets) {
-        case 64: return launch_pipe_tile<64>(m, s, b, model, t_offset, grid, st);
-        case 128: return launch_pipe_tile<128>(m, s, b, model, t_offset, grid, st);
-        case 256: return launch_pipe_tile<256>(m, s, b, model, t_offset, grid, st);
-        default: return cudaErrorInvalidValue;
-    }
-}
-
 template <int TILE>
 static cudaError_t launch_tile(const MeshDev& m, const StateDev& s, const BatchDev& b, int model, int t_offset,
                                cudaStream_t st) {

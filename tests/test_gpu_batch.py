@@ -22,7 +22,6 @@ def test_batch_equals_cells_run_alone_bitwise(monkeypatch):
     """Same tile size as the plain path's default (128): same plans, and the same kernels (the
     plain path is a one-cell table), so every cell's state and curve match bit for bit."""
     monkeypatch.delenv("NFX_TILE_TETS", raising=False)
-    monkeypatch.delenv("NFX_TET_KERNEL", raising=False)
     cells = small_population()
     meshes = [w.mesh() for w in cells]
     b = Batch(0, tile_tets=128)
