@@ -50,7 +50,7 @@ extern "C" {
 #define NFX_STATUS_NONFINITE 1u  /* a position/velocity/force became NaN or Inf (util/IO.py:17-28 aborts on this) */
 #define NFX_STATUS_INVERTED 2u   /* an element reached det F <= 0 */
 #define NFX_STATUS_CURVE_FULL 4u /* a force-curve row fell outside the buffer given to nfx_set_record */
-#define NFX_STATUS_TIMEOUT 8u    /* a bounded wait on an asynchronous copy gave up (the step is invalid) */
+#define NFX_STATUS_TIMEOUT 8u    /* reserved: a bounded device wait gave up (the step is invalid); no current kernel waits */
 
 /* per-tetra fields (nfx_get_tet_field) */
 #define NFX_FIELD_VON_MISES 0   /* vonMises buffer, Simulation.py:89 */

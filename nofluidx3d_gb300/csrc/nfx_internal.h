@@ -32,10 +32,10 @@ constexpr float FORCE_FIX_MAX = 4.0e6f;  // larger tile sums raise STATUS_NONFIN
 constexpr unsigned STATUS_NONFINITE = 1u;   // a position or force became NaN/Inf
 constexpr unsigned STATUS_INVERTED = 2u;    // an element reached det F <= 0
 constexpr unsigned STATUS_CURVE_FULL = 4u;  // a record row fell outside the curve buffer
-constexpr unsigned STATUS_TIMEOUT = 8u;     // a bounded wait on an asynchronous copy gave up
+constexpr unsigned STATUS_TIMEOUT = 8u;     // reserved: a bounded device wait gave up (no current kernel waits)
 
-// Extra elements allocated after every per-tetra array and the tile node list: bulk copies
-// round their sizes up to 16 bytes and may read that far past a tile's last element.
+// Extra zeroed elements after every per-tetra array and the tile node list (slack for loads
+// that run past a tile's last real element).
 constexpr int ARRAY_PAD = 16;
 
 // ---------------------------------------------------------------------------------------
