@@ -62,6 +62,14 @@ typedef struct nfx_sim nfx_sim;
 /* Library version, e.g. 100 for 0.1.0. */
 int nfx_version(void);
 
+/* Builds the device layout plan of a mesh on the host (no GPU needed) and checks its invariants:
+ * every tetra in exactly one tile slot, tile sizes within bounds, corners naming the right
+ * nodes, each node's incidence run holding exactly its corners in (tetra, corner) order, runs
+ * ordered by decreasing length. Returns the tile count and the number of node entries over all
+ * tiles. A planner self-check with no counterpart in the reference. */
+int nfx_plan_check(int64_t np, int64_t nt, const double* points, const uint32_t* tets, int tile_tets,
+                   int64_t* ntiles, int64_t* node_entries);
+
 /* Copies the last error message of this thread into buf (NUL-terminated, truncated to len).
  * Replaces the reference's print()+exit() error paths (openCL.py:30-32, util/IO.py:17-28). */
 int nfx_last_error(char* buf, size_t len);

@@ -37,6 +37,7 @@ _vp = C.c_void_p
 _i64 = C.c_int64
 _SIGS = {
     "nfx_version": ([], C.c_int),
+    "nfx_plan_check": ([_i64, _i64, _vp, _vp, C.c_int, C.POINTER(_i64), C.POINTER(_i64)], C.c_int),
     "nfx_last_error": ([C.c_char_p, C.c_size_t], C.c_int),
     "nfx_create": ([C.c_int, C.POINTER(_vp)], C.c_int),
     "nfx_destroy": ([_vp], C.c_int),

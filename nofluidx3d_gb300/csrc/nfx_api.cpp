@@ -214,6 +214,60 @@ extern "C" {
 
 int nfx_version(void) { return 100; }
 
+int nfx_plan_check(int64_t np, int64_t nt, const double* points, const uint32_t* tets, int tile_tets,
+                   int64_t* ntiles, int64_t* node_entries) {
+    CHECK_ARG(points && tets && ntiles && node_entries, "null argument");
+    MeshPlan P;
+    std::string err;
+    if (!build_mesh_plan(np, nt, points, tets, tile_tets, P, err)) return fail(NFX_ERR_ARG, err);
+    const int64_t T = P.tile_tets, NM = std::min<int64_t>(T, TILE_NODES_MAX);
+    auto bad = [&](const std::string& what) { return fail(NFX_ERR_STATE, "plan_check: " + what); };
+    if (P.nslots != P.ntiles * T || (int64_t)P.tile_meta.size() != P.ntiles) return bad("tile counts");
+    std::vector<int> seen((size_t)nt, 0);
+    int64_t entries = 0;
+    for (int64_t b = 0; b < P.ntiles; b++) {
+        const int64_t ntt = P.tile_meta[b] & 0xffffu, nn = P.tile_meta[b] >> 16;
+        if (ntt < 1 || ntt > T || nn < 1 || nn > NM) return bad("tile " + std::to_string(b) + " sizes");
+        entries += nn;
+        std::vector<int> uses((size_t)nn, 0);
+        for (int64_t j = 0; j < T; j++) {
+            const int64_t slot = b * T + j, ut = P.tet_user[slot];
+            if (j >= ntt) {
+                if (ut != -1) return bad("padding slot holds a tetra");
+                continue;
+            }
+            if (ut < 0 || ut >= nt || seen[ut]++) return bad("tetra missing or repeated");
+            for (int k = 0; k < 4; k++) {
+                const int64_t loc = P.lconn[4 * slot + k];
+                if (loc >= nn) return bad("corner index past the tile's nodes");
+                const uint32_t id = P.tile_nodes[2 * (b * NM + loc)];
+                if (P.node_user[id] != (int64_t)tets[k * nt + ut]) return bad("corner names the wrong node");
+                uses[loc]++;
+            }
+        }
+        // incidence list: node q's run holds exactly its corners, as corner-major slots, in order
+        uint32_t prev_count = 0xffffffffu;
+        for (int64_t q = 0; q < nn; q++) {
+            const uint32_t w = P.tile_nodes[2 * (b * NM + q) + 1], first = w >> 16, count = w & 0xffffu;
+            if ((int)count != uses[q] || count > prev_count) return bad("incidence counts");
+            prev_count = count;
+            int last = -1;
+            for (uint32_t e = 0; e < count; e++) {
+                const uint32_t v = P.tile_inc[4 * b * T + first + e], k = v / T, j = v % T;
+                if ((int64_t)j >= ntt || P.lconn[4 * (b * T + j) + k] != q) return bad("incidence entry");
+                const int order = (int)(4 * j + k);
+                if (order <= last) return bad("incidence order");
+                last = order;
+            }
+        }
+    }
+    for (int64_t t = 0; t < nt; t++)
+        if (seen[t] != 1) return bad("tetra not covered");
+    *ntiles = P.ntiles;
+    *node_entries = entries;
+    return NFX_OK;
+}
+
 int nfx_last_error(char* buf, size_t len) {
     if (!buf || len == 0) return NFX_ERR_ARG;
     std::snprintf(buf, len, "%s", g_err.c_str());

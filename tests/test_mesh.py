@@ -82,3 +82,40 @@ def test_batched_walls_start_tangent(R):
     assert d.min() >= sph["radius"] - 1e-12
     with pytest.raises(ValueError):
         w.contacts()  # d0 = None needs the mesh
+
+
+def _plan_check(points: np.ndarray, tets: np.ndarray, tile: int) -> tuple[int, int]:
+    import ctypes as C
+
+    from nofluidx3d_gb300 import _lib
+
+    L = _lib.load()
+    P = np.ascontiguousarray(np.asarray(points, np.float64).T)   # SoA x..., y..., z...
+    T = np.ascontiguousarray(np.asarray(tets, np.uint32).T)      # SoA corner 0..., 1..., 2..., 3...
+    a, b = C.c_int64(), C.c_int64()
+    _lib.check(L.nfx_plan_check(P.shape[1], T.shape[1], P.ctypes.data_as(C.c_void_p), T.ctypes.data_as(C.c_void_p),
+                                tile, C.byref(a), C.byref(b)))
+    return a.value, b.value
+
+
+@pytest.mark.parametrize("tile", [64, 128, 256, 512])
+def test_tile_plan_invariants(tile):
+    """The host planner's tiles cover every tetra once, name the right nodes, and hold each node's
+    corners in its incidence run (checked inside nfx_plan_check); region-grown tiles stay compact."""
+    m = kuhn_sphere(12.0, 0.02, 0)
+    ntiles, entries = _plan_check(m.points, m.tets, tile)
+    # tiles close early only at the end of the curve or when the node cap binds (512-tetra tiles
+    # have 256 node entries): at least 98 % of the slots hold a tetra
+    assert -(-m.num_tetra // tile) <= ntiles and m.num_tetra / (ntiles * tile) > 0.98
+    # each node entry of a tile costs a gather and three atomics; compact tiles share few nodes
+    # (measured at R = 12: 0.605, 0.498, 0.421, 0.362 entries per tetra)
+    assert entries / m.num_tetra < {64: 0.65, 128: 0.53, 256: 0.45, 512: 0.39}[tile]
+
+
+def test_tile_plan_any_tetra_order():
+    """Shuffled tetra order and a single tetra: the same invariants hold."""
+    m = kuhn_sphere(6.0, 0.02, 1)
+    rng = np.random.default_rng(5)
+    _plan_check(m.points, np.asarray(m.tets)[rng.permutation(m.num_tetra)], 128)
+    one = np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.0, 0.0, 1.0]])
+    assert _plan_check(one, np.array([[0, 1, 2, 3]]), 128) == (1, 4)
