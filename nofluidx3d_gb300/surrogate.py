@@ -19,7 +19,7 @@ gradient descent through the network (many starts per target, no simulation), ha
 verify each proposal, and refines it by defect correction (output space mapping): the target is
 shifted by the simulator-minus-network difference at the current point and the network's inputs
 are refitted to the shifted target, one verifying simulation per iteration, for as long as the
-simulated error keeps improving. The simulator is the judge of every reported error.
+simulated error keeps improving. Every reported error is measured against the simulator.
 
 The reference has no learned part; curves come from the batched simulator (core.Batch), whose
 cells evolve bit for bit as the plain path (core.CellSim) runs them alone.
