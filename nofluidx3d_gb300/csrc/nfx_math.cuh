@@ -349,7 +349,8 @@ NFX_HD void vp_element(const float d1[3], const float d2[3], const float d3[3], 
 #pragma unroll
     for (int k = 0; k < 9; k++) Pm.m[k] = Pp[k];
     const Mat3 adjFp = adj_1p(Pm);
-    const float rdet = fdiv_(1.0f, 1.0f + det1p_minus1(Pm));
+    // det(I + P) by expansion along the first row of the adjugate already formed
+    const float rdet = fdiv_(1.0f, (1.0f + Pm.m[0]) * adjFp.m[0] + Pm.m[1] * adjFp.m[3] + Pm.m[2] * adjFp.m[6]);
     Mat3 D;
 #pragma unroll
     for (int k = 0; k < 9; k++) D.m[k] = H.m[k] - Pm.m[k];
@@ -377,15 +378,24 @@ NFX_HD void vp_element(const float d1[3], const float d2[3], const float d3[3], 
     const float sigma0 = par.yield * (par.hard_exp == 0.0f ? 1.0f : pow_(1.0f + eps / par.hard_thr, par.hard_exp));
     vm_out = vm;
     p_out = t3;
-    const float ratio = fdiv_(vm, sigma0);
-    const float rate = par.flow_rate * (par.flow_exp == 1.0f ? ratio : pow_(ratio, par.flow_exp));
+    // linear flow law: rate / vm is the constant flow_rate / sigma0 (one division)
+    float rate, kv;
+    if (par.flow_exp == 1.0f) {
+        const float q = fdiv_(par.flow_rate, sigma0);
+        rate = q * vm;
+        kv = 1.5f * q;
+    } else {
+        rate = par.flow_rate * pow_(fdiv_(vm, sigma0), par.flow_exp);
+        kv = vm != 0.0f ? fdiv_(rate * 1.5f, vm) : 0.0f;
+    }
     rate_out = rate;
 #pragma unroll
     for (int q = 0; q < 9; q++) dP[q] = 0.0f;
     if (vm != 0.0f) {
-        const float k = fdiv_(rate * 1.5f, vm);
+        const float rJ = fdiv_(1.0f, 1.0f + JFm1);
+        const float k = kv * rJ;  // 1/det F folded into the scale of Dp
         const float Dp[9] = {dxx * k, s.xy * k, s.xz * k, s.xy * k, dyy * k, s.yz * k, s.xz * k, s.yz * k, dzz * k};
-        // T = adj(F) Dp, then M = T (I + H) / det F
+        // T = adj(F) Dp / det F (the 1/det F inside k), then M = T (I + H)
         float T[9];
 #pragma unroll
         for (int i = 0; i < 3; i++) {
@@ -393,14 +403,13 @@ NFX_HD void vp_element(const float d1[3], const float d2[3], const float d3[3], 
             for (int j = 0; j < 3; j++)
                 T[3 * i + j] = A.m[3 * i] * Dp[j] + A.m[3 * i + 1] * Dp[3 + j] + A.m[3 * i + 2] * Dp[6 + j];
         }
-        const float rJ = fdiv_(1.0f, 1.0f + JFm1);
         float M[9];
 #pragma unroll
         for (int i = 0; i < 3; i++) {
 #pragma unroll
             for (int j = 0; j < 3; j++)
-                M[3 * i + j] = (T[3 * i + j] + (T[3 * i] * H.m[j] + T[3 * i + 1] * H.m[3 + j] +
-                                                T[3 * i + 2] * H.m[6 + j])) * rJ;
+                M[3 * i + j] = T[3 * i + j] + (T[3 * i] * H.m[j] + T[3 * i + 1] * H.m[3 + j] +
+                                               T[3 * i + 2] * H.m[6 + j]);
         }
         // dP = (I + P) M
 #pragma unroll

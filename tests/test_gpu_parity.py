@@ -201,7 +201,7 @@ def test_sphere_integral_readout_in_step_equals_on_demand():
 def test_gpu_viscoplastic_sphere_10k_steps_vs_fp64_oracle():
     """R=8 Mooney-Rivlin + viscoplastic cell under a sphere of radius 2, 10^4 steps, against the
     FP64 oracle, at the bars of 1e-5 (trajectories) and 1e-4 (force curve). Measured on GB300:
-    trajectory 4.7e-7, curve 9.3e-5 L2, where a direct FP32 port of the reference reaches 1.8e-5
+    trajectory 4.7e-7, curve 9.6e-5 L2, where a direct FP32 port of the reference reaches 1.8e-5
     and 1.4e-2 (and the same kernels with the unrefined fast divide 1.03e-4)."""
     from nofluidx3d_gb300.workloads import plain_large
 
