@@ -3,7 +3,7 @@
  *
  * One nfx_sim handle is one cell simulation on one GPU: it owns the device buffers the
  * reference's Simulation and its Interaction plugins own (nofluidx3d/Simulation.py:82-90,
- * nofluidx3d/interactions/*.py createBuffers) and runs the whole step — element forces, node
+ * createBuffers of the plugins in nofluidx3d/interactions/) and runs the whole step — element forces, node
  * force accumulation, contacts, velocity Verlet, indenter-force readout — as CUDA kernels.
  *
  * Layout conventions are the reference's, so its Bridge host arrays (nofluidx3d/util/Bridge.py:16-26)

@@ -85,7 +85,7 @@ int set_device(nfx_sim* s) {
 }
 
 template <class T>
-int dalloc(nfx_sim* s, T** p, size_t count, std::vector<void*>* owner) {
+int dalloc(nfx_sim* /*s*/, T** p, size_t count, std::vector<void*>* owner) {
     void* q = nullptr;
     cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
     if (e != cudaSuccess) return fail(NFX_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
