@@ -19,6 +19,10 @@ INCLUDE = PKG.parent / "include"
 BUILD_DIR = PKG / "_build"
 LIB_NAME = "libnfx.so"
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Device code generation: ptxas's least register-hungry allocation bias. At the 64-register cap
+# of the element pass it leaves no spills and measured 0.6 % faster steps than the default level
+# (level 8-10 1 % slower); it does not change the arithmetic.
+DEVICE_FLAGS = ["-Xptxas=--register-usage-level=0"]
 
 SOURCES = ["nfx_kernels.cu", "nfx_noalloc.cu", "nfx_mlp.cu", "nfx_api.cpp", "nfx_mesh.cpp", "nfx_batch.cpp"]
 HEADERS = ["nfx_internal.h", "nfx_math.cuh"]
@@ -70,7 +74,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         obj = BUILD_DIR / (Path(src).stem + ".o")
         objs.append(obj)
         if src.endswith(".cu"):
-            cmd = [nvcc, *ARCH_FLAGS, "-lineinfo", *common, "-c", str(CSRC / src), "-o", str(obj)]
+            cmd = [nvcc, *ARCH_FLAGS, *DEVICE_FLAGS, "-lineinfo", *common, "-c", str(CSRC / src), "-o", str(obj)]
         else:
             cmd = [nvcc, *common, "-x", "c++", "-c", str(CSRC / src), "-o", str(obj)]
         if verbose:
