@@ -147,12 +147,12 @@ __device__ __forceinline__ float fix_to_float(unsigned long long w) {
 
 // One tile node: sum its corner forces in the tile's fixed incidence order and add the sum to
 // the global accumulator as 64-bit fixed point, so the total does not depend on the order in
-// which tiles finish. Incidence entries are corner-force slots (corner * TILE + local tet). The
-// loop takes four corners per iteration (their loads issued together; 2.7 % faster element pass
-// than one at a time at R = 64), adding them in list order all the same. Returns false when the
-// sum is out of the fixed-point range (nothing is added then).
+// which tiles finish. Incidence entries are corner-force slots (corner * TILE + local tet). One
+// corner per iteration at the 56-register budget (NFX_FLUSH_UNROLL=4 takes four per iteration,
+// in the same order: faster at 64 registers, 5 % slower at 56). Returns false when the sum is out
+// of the fixed-point range (nothing is added then).
 #ifndef NFX_FLUSH_UNROLL
-#define NFX_FLUSH_UNROLL 4  // 1: one corner per iteration
+#define NFX_FLUSH_UNROLL 1
 #endif
 template <int TILE>
 __device__ __forceinline__ bool node_flush(uint2 node, const unsigned short* inc, const float4* s_cf,
@@ -284,7 +284,7 @@ __device__ __forceinline__ double tile_sum(float v, double* s_scratch) {
 // The tile's material comes from its cell's entry in the cell table (cell 0 when the table has
 // no tile map), so a single simulation and a batch run this same code.
 #ifndef NFX_TET_REGS
-#define NFX_TET_REGS 64  // registers per thread the element pass is compiled for (8 CTAs of 128 per SM)
+#define NFX_TET_REGS 56  // registers per thread of the element pass: 9 CTAs of 128 per SM (64: 8)
 #endif
 #ifndef NFX_DMI_FROM_X
 #define NFX_DMI_FROM_X 0  // 1: Dm^-1 and V0 from the staged reference positions instead of the stored arrays
