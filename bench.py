@@ -314,7 +314,8 @@ def run_batched(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--steps", type=int, default=8000,
+                    help="timed steps (8000 at R=64: about 2 s, ten clock samples)")
     ap.add_argument("--warmup", type=int, default=200)
     ap.add_argument("--impl", default="nfx", choices=["nfx", "reference"])
     ap.add_argument("--workload", default="plain-large", choices=sorted(workloads.WORKLOADS))
