@@ -10,8 +10,10 @@ descending 1e-4 per step, damping 1e-2, FP32 kernels. A "step" is one time step 
              events on the library's stream (nfx_time_steps); whole job over all ranks.
   e2e        the same metric through the C ABI with host buffers: per output interval of 100
              steps the indenter positions are uploaded from pinned host memory (the reference's
-             per-step beforeTimeStep callable) and node positions plus the force row are read
-             back into pinned host memory (the reference's writeVTK readback).
+             per-step beforeTimeStep callable), and the node positions plus the recorded force
+             rows come back into pinned host memory (the reference's writeVTK readback) through
+             output snapshots (nfx_snapshot) whose copies run while the next interval computes;
+             the host waits for every interval's output.
   roofline   the element pass (dominant kernel): algorithmic bytes per launch / its average
              launch duration, from --tet-launches back-to-back launches between two CUDA events
              (nfx_profile_tet_pass), against MEASURED_PEAKS.json hbm_gbs. The per-step
@@ -379,27 +381,37 @@ def main():
     # end to end through the C ABI with pinned host buffers
     import torch
 
-    pos_host = torch.empty(3 * npn, dtype=torch.float64, pin_memory=True).numpy()
-    tab_host = torch.empty(w.record_every, dtype=torch.float64, pin_memory=True).numpy()
+    # two sets of pinned host buffers: the host reads interval k's output (snapshot) while the
+    # device runs interval k + 1
+    pos_host = [torch.empty(3 * npn, dtype=torch.float64, pin_memory=True).numpy() for _ in range(2)]
+    rows_host = [torch.empty((total // w.record_every + 2, 3), dtype=torch.float64, pin_memory=True).numpy()
+                 for _ in range(2)]
+    tab_host = [torch.empty(w.record_every, dtype=torch.float64, pin_memory=True).numpy() for _ in range(2)]
     c = w.contacts(mesh)[w.record_contact]
     intervals = max(1, args.e2e_steps // w.record_every)
     barrier(dist, local)
     sim.sync()
     t0 = time.perf_counter()
-    for _ in range(intervals):
+    n_rows = 0
+    d2h_bytes = 0.0
+    for k in range(intervals):
         t = sim.time
         tt = np.arange(t, t + w.record_every, dtype=np.float64)
-        tab_host[:] = c["p0"] - c["v"] * tt  # the host-side position callable
-        sim.set_contact_table(w.record_contact, t, tab_host)
+        tab_host[k % 2][:] = c["p0"] - c["v"] * tt  # the host-side position callable
+        sim.set_contact_table(w.record_contact, t, tab_host[k % 2])
         sim.step(w.record_every)
-        sim.points_soa(out=pos_host)
-        _ = sim.curve()[-1]
+        if k > 0:
+            sim.snapshot_wait()  # interval k - 1's positions and force rows are on the host
+            _ = rows_host[(k - 1) % 2][n_rows - 1] if n_rows else None
+        n_rows = sim.snapshot(pos_host[k % 2], rows_host[k % 2])
+        d2h_bytes += 8.0 * 3 * npn + 24.0 * min(n_rows, rows_host[0].shape[0])
+    sim.snapshot_wait()
     sim.sync()
     e2e_s = reduce_max(dist, time.perf_counter() - t0, local)
     e2e_steps = intervals * w.record_every
     e2e_val = world * nt * e2e_steps / e2e_s
     h2d = 8.0 * w.record_every * intervals / e2e_steps + 16.0 / w.record_every
-    d2h = (8.0 * 3 * npn + 24.0) / w.record_every
+    d2h = d2h_bytes / e2e_steps
     status = sim.status()
 
     if rank != 0:

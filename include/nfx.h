@@ -139,6 +139,19 @@ int nfx_step(nfx_sim* sim, int64_t nsteps);
  * the readout the reference makes after the last step of a run (Simulation.py:274-278). */
 int nfx_record_now(nfx_sim* sim);
 
+/* Output snapshot without draining the step stream, for callers that write frames while the
+ * simulation continues. Enqueues, after the steps enqueued so far, the node positions (user
+ * order, SoA, as nfx_get_points) into `points_out` and the force rows recorded so far (up to
+ * max_rows, as nfx_get_curve) into `rows_out`; returns at once with the number of recorded rows
+ * in *n_rows. The host copies run on a second stream while later steps run; the buffers are
+ * written asynchronously (page-locked host memory keeps the copies asynchronous) and may be read
+ * only after nfx_snapshot_wait. A new snapshot may be taken before waiting for the previous one
+ * (its device staging waits for the previous copy); nfx_snapshot_wait waits for the latest. The
+ * reference reads positions synchronously at every output (util/IO.py:15); this is the
+ * overlapped form of that readback. */
+int nfx_snapshot(nfx_sim* sim, double* points_out, double* rows_out, int64_t max_rows, int64_t* n_rows);
+int nfx_snapshot_wait(nfx_sim* sim);
+
 /* Waits for all enqueued work of the handle. */
 int nfx_sync(nfx_sim* sim);
 

@@ -69,6 +69,8 @@ _SIGS = {
     "nfx_profile_steps": ([_vp, _i64, C.POINTER(C.c_float), C.POINTER(C.c_float)], C.c_int),
     "nfx_profile_tet_pass": ([_vp, C.c_int, C.POINTER(C.c_float)], C.c_int),
     "nfx_mesh_info": ([_vp, C.POINTER(_i64), C.POINTER(_i64)], C.c_int),
+    "nfx_snapshot": ([_vp, _vp, _vp, _i64, C.POINTER(_i64)], C.c_int),
+    "nfx_snapshot_wait": ([_vp], C.c_int),
     "nfx_divide_check": ([C.c_int, _i64, _vp, _vp, _vp], C.c_int),
     "nfx_indenter_force_noalloc": ([C.c_int, _i64, _vp, C.c_int, C.c_double, C.c_double, C.c_double, _vp, _vp],
                                    C.c_int),

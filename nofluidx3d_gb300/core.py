@@ -125,6 +125,24 @@ class CellSim:
     def sync(self) -> None:
         check(self._L.nfx_sync(self._h))
 
+    def snapshot(self, points_out: np.ndarray, rows_out: np.ndarray | None = None) -> int:
+        """Start an asynchronous copy of the node positions (SoA, 3*np doubles) and the recorded
+        force rows (rows_out: [max_rows, 3] doubles) taken after the steps enqueued so far; later
+        steps may be enqueued at once. Read the buffers only after snapshot_wait(). Returns the
+        number of rows recorded so far."""
+        assert points_out.dtype == np.float64 and points_out.flags.c_contiguous and points_out.size == 3 * self.np
+        rows = 0 if rows_out is None else rows_out.shape[0]
+        if rows_out is not None:
+            assert rows_out.dtype == np.float64 and rows_out.flags.c_contiguous and rows_out.shape[1:] == (3,)
+        n = C.c_int64()
+        check(self._L.nfx_snapshot(self._h, _ptr(points_out), None if rows_out is None else _ptr(rows_out), rows,
+                                   C.byref(n)))
+        return n.value
+
+    def snapshot_wait(self) -> None:
+        """Wait for the copies of the latest snapshot."""
+        check(self._L.nfx_snapshot_wait(self._h))
+
     @property
     def time(self) -> int:
         t = C.c_int64()

@@ -75,6 +75,12 @@ struct nfx_sim {
     cudaGraphExec_t graph = nullptr;
     bool graph_valid = false;
     int tile_tets = DEFAULT_TILE_TETS;     // tetrahedra per tile (64, 128, 256 or 512)
+    // asynchronous output snapshots (nfx_snapshot): positions staged on the step stream, copied
+    // to the host on a second stream while later steps run
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_snap = nullptr, ev_copy = nullptr;
+    double* d_snap = nullptr;  // 3 * np doubles, allocated with the first snapshot of a mesh
+    bool snap_pending = false;
 };
 
 namespace {
@@ -94,7 +100,19 @@ int dalloc(nfx_sim* /*s*/, T** p, size_t count, std::vector<void*>* owner) {
     return NFX_OK;
 }
 
+// Waits for the copies of the last snapshot (before its staging or the curve buffer is freed or
+// reset).
+void snapshot_drain(nfx_sim* s) {
+    if (s->snap_pending) {
+        cudaEventSynchronize(s->ev_copy);
+        s->snap_pending = false;
+    }
+}
+
 void free_mesh(nfx_sim* s) {
+    snapshot_drain(s);
+    if (s->d_snap) cudaFree(s->d_snap);
+    s->d_snap = nullptr;
     for (void* p : s->mesh_allocs) cudaFree(p);
     s->mesh_allocs.clear();
     s->mesh = MeshDev{};
@@ -325,6 +343,9 @@ int nfx_destroy(nfx_sim* s) {
     if (s->stream) cudaStreamSynchronize(s->stream);
     invalidate_graph(s);
     free_mesh(s);
+    if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
+    if (s->ev_snap) cudaEventDestroy(s->ev_snap);
+    if (s->ev_copy) cudaEventDestroy(s->ev_copy);
     for (int c = 0; c < MAX_CONTACTS; c++) {
         if (s->d_tables[c]) cudaFree(s->d_tables[c]);
         if (s->d_meta[c]) cudaFree(s->d_meta[c]);
@@ -600,6 +621,7 @@ int nfx_set_record(nfx_sim* s, int contact, int64_t every, int64_t max_rows) {
     int rc;
     if ((rc = set_device(s)) != NFX_OK) return rc;
     CUDA_TRY(cudaStreamSynchronize(s->stream));
+    snapshot_drain(s);
     if (contact >= 0 && max_rows > s->curve_rows) {
         if (s->d_curve) cudaFree(s->d_curve);
         s->d_curve = nullptr;
@@ -773,6 +795,47 @@ int nfx_get_curve(nfx_sim* s, double* rows, int64_t max_rows, int64_t* n_rows) {
     }
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     *n_rows = s->rows_written;
+    return NFX_OK;
+}
+
+int nfx_snapshot(nfx_sim* s, double* points_out, double* rows_out, int64_t max_rows, int64_t* n_rows) {
+    CHECK_ARG(s && points_out && n_rows, "null argument");
+    CHECK_ARG(max_rows >= 0 && (max_rows == 0 || rows_out), "bad row buffer");
+    if (!s->have_mesh) return fail(NFX_ERR_STATE, "no mesh");
+    int rc;
+    if ((rc = set_device(s)) != NFX_OK) return rc;
+    if (!s->copy_stream) {
+        CUDA_TRY(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking));
+        CUDA_TRY(cudaEventCreateWithFlags(&s->ev_snap, cudaEventDisableTiming));
+        CUDA_TRY(cudaEventCreateWithFlags(&s->ev_copy, cudaEventDisableTiming));
+    }
+    const size_t bytes = 3 * (size_t)s->plan.np * sizeof(double);
+    if (!s->d_snap && (rc = dalloc(s, &s->d_snap, 3 * (size_t)s->plan.np, nullptr)) != NFX_OK) return rc;
+    // the previous snapshot's copy must have left the staging buffer before it is rewritten
+    if (s->snap_pending) CUDA_TRY(cudaStreamWaitEvent(s->stream, s->ev_copy, 0));
+    CUDA_TRY(launch_points_to_user(s->mesh, s->st, s->d_node_user, s->d_snap, s->stream));
+    CUDA_TRY(cudaEventRecord(s->ev_snap, s->stream));
+    CUDA_TRY(cudaStreamWaitEvent(s->copy_stream, s->ev_snap, 0));
+    CUDA_TRY(cudaMemcpyAsync(points_out, s->d_snap, bytes, cudaMemcpyDeviceToHost, s->copy_stream));
+    // rows already recorded are final: later steps only write rows after them
+    const long long n = std::min<long long>(s->rows_written, max_rows);
+    if (n > 0)
+        CUDA_TRY(cudaMemcpyAsync(rows_out, s->d_curve, 3 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost,
+                                 s->copy_stream));
+    CUDA_TRY(cudaEventRecord(s->ev_copy, s->copy_stream));
+    s->snap_pending = true;
+    *n_rows = s->rows_written;
+    return NFX_OK;
+}
+
+int nfx_snapshot_wait(nfx_sim* s) {
+    CHECK_ARG(s, "null handle");
+    int rc;
+    if ((rc = set_device(s)) != NFX_OK) return rc;
+    if (!s->snap_pending) return NFX_OK;
+    const cudaError_t e = cudaEventSynchronize(s->ev_copy);
+    s->snap_pending = false;
+    if (e != cudaSuccess) return fail(NFX_ERR_CUDA, std::string("snapshot: ") + cudaGetErrorString(e));
     return NFX_OK;
 }
 
