@@ -389,6 +389,9 @@ def main():
     tab_host = [torch.empty(w.record_every, dtype=torch.float64, pin_memory=True).numpy() for _ in range(2)]
     c = w.contacts(mesh)[w.record_contact]
     intervals = max(1, args.e2e_steps // w.record_every)
+    # the first snapshot creates the copy stream, its events and the staging buffer: not timed
+    sim.snapshot(pos_host[1], rows_host[1])
+    sim.snapshot_wait()
     barrier(dist, local)
     sim.sync()
     t0 = time.perf_counter()
