@@ -19,6 +19,15 @@ descending 1e-4 per step, damping 1e-2, FP32 kernels. A "step" is one time step 
              (nfx_profile_tet_pass), against MEASURED_PEAKS.json hbm_gbs. The per-step
              launch-by-launch event profile (nfx_profile_steps) is reported beside it in config;
              its brackets add the event overhead to every kernel.
+  e2e_api    the same metric through the reference-facing Python surface (Simulation with the
+             Substrate, Sphere, FiniteStrainViscoplastic and VelocityVerlet plugins): the sphere's
+             position is a plain Python callable evaluated on the host for every step and uploaded
+             as a position table, and every output interval reads the positions back as
+             Simulation.run does (file writing off).
+  roofline_1m  the element pass's roofline on the 1M-tetra cell (R = 34, 989,808 tetra).
+  batched    the batched population (256 cells, R ~ logU[6, 40], per-cell materials) advanced as
+             one batch against looping the plain path over the same cells: sims/s, speed-up,
+             tile size per size bucket.
   cpu_baseline  the oracle port of the reference kernels (FP64, OpenMP, all host cores) on a
              bounded sample of the same workload.
 
@@ -219,8 +228,11 @@ def run_reference(args):
     mesh = w.mesh()
     st = O.State(oracle_problem(w, mesh), "f64")
     th = O.max_threads()
-    for _ in range(min(args.warmup, 1)):
+    t0 = time.perf_counter()
+    for _ in range(args.warmup):  # the requested warm-up, unless it would take more than a third of the budget
         st.run(1, parallel=True, threads=th)
+        if time.perf_counter() - t0 > args.reference_seconds / 3:
+            break
     budget = args.reference_seconds
     done, t0 = 0, time.perf_counter()
     while done < args.steps and (time.perf_counter() - t0) < budget:
@@ -230,10 +242,10 @@ def run_reference(args):
     val = mesh.num_tetra * done / dt
     line = {
         "impl": "reference", "metric": METRIC, "value": val, "unit": "tetra-steps/s", "n_gpus": world,
-        "steps": done, "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * dt / max(done, 1),
+        "steps": done, "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(done, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": w.name, "tets": mesh.num_tetra, "nodes": mesh.num_points,
-                   "implementation": "oracle port of the reference's OpenCL kernels, OpenMP"},
+        "config": bench_config(w, mesh.num_tetra, mesh.num_points, world),
+        "implementation": "oracle port of the reference's OpenCL kernels, OpenMP",
         "cpu_baseline": {"value": val, "unit": "tetra-steps/s", "cores": th, "kind": "port",
                          "sample": f"{done} whole time steps (of {args.steps} requested, capped at {budget:.0f} s)"},
         "e2e": {"value": val, "unit": "tetra-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -244,18 +256,24 @@ def run_reference(args):
 METRIC = "tetra-steps/s + % HBM peak, 1 GB300"
 
 
-def run_batched(args):
+def bench_config(w, nt: int, npn: int, world: int) -> dict:
+    """The workload description both arms print (identical for the same workload)."""
+    return {"workload": w.name, "tets": nt, "nodes": npn, "parallelism": "replicas" if world > 1 else "single",
+            "l2": f"inputs larger than L2: {(ELEM_BYTES[w.material] * nt + NODE_BYTES * npn) / 1e6:.0f} MB "
+                  "of algorithmic state streamed per step vs 129 MB L2"}
+
+
+def batched_measure(args, world, rank, local, dist, steps: int, warmup: int) -> dict | None:
     """Batched population (256 cells, radius log-uniform in [6, 40] unless --batch-rmin/--batch-rmax
     say otherwise, per-cell materials): steps/s of one batch advancing every cell, against looping
     the plain path over the same cells (each cell's plain step time measured on that cell through
     nfx_step in CUDA-graph chunks, summed). sims/s = cells / (20k steps' time). Under torchrun the
     cells are split across ranks by LPT on their tetra counts (no data-path collective); times are
-    the maximum over ranks."""
+    the maximum over ranks. Returns the JSON line on rank 0 (None elsewhere)."""
     from nofluidx3d_gb300.core import Batch, CellSim
     from nofluidx3d_gb300.mesh import mesh_counts
     from nofluidx3d_gb300.shard import lpt_partition
 
-    world, rank, local, dist = dist_setup()
     r_range = (args.batch_rmin, args.batch_rmax)
     all_cells = workloads.batched_cells(args.batch_cells, seed=0, r_range=r_range)
     n_all = len(all_cells)
@@ -269,22 +287,30 @@ def run_batched(args):
     b = Batch(local, tile_tets=args.batch_tile)
     for w, m in zip(cells, meshes):
         w.add_to_batch(b, m)
-    b.set_record(1, 100, args.warmup + args.steps + 10)
+    b.set_record(1, 100, warmup + steps + 60)
     b.finalize()
     t_setup = time.perf_counter() - t0
-    b.time_steps(max(args.warmup, 50))  # at least one 50-step chunk, so its graph exists before timing
+    b.time_steps(max(warmup, 50))  # at least one 50-step chunk, so its graph exists before timing
     barrier(dist, local)
-    ms = reduce_max(dist, b.time_steps(args.steps), local)
-    batch_step_ms = ms / args.steps
+    ms = reduce_max(dist, b.time_steps(steps), local)
+    batch_step_ms = ms / steps
     status = b.status()
     cell_status = b.cell_status()
     info = b.info()
     b.close()
-    # looped plain path: each cell alone, a short timed run per cell
-    plain_ms = []
-    for w, m in zip(cells, meshes):
+    # looped plain path: each cell alone, a short timed run per cell. The cells' handles are set up
+    # on host threads (each builds its own plan in native code), then timed one after another.
+    from concurrent.futures import ThreadPoolExecutor
+
+    def make(wm):
         s = CellSim(local)
-        w.configure(s, m, max_rows=4)
+        wm[0].configure(s, wm[1], max_rows=4)
+        return s
+
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
+        sims = list(ex.map(make, zip(cells, meshes)))
+    plain_ms = []
+    for s in sims:
         s.time_steps(100)  # warm-up that also captures the cell's 100-step graph
         plain_ms.append(s.time_steps(args.loop_steps) / args.loop_steps)
         s.close()
@@ -292,16 +318,17 @@ def run_batched(args):
     status = int(reduce_max(dist, float(status), local))
     n_bad = int(reduce_max(dist, float((cell_status != 0).sum()), local))
     if rank != 0:
-        return
+        return None
     n, nt = n_all, nt_all
     sim_steps = 20000
     line = {
         "metric": f"batched sims/s ({n} cells, 20k steps)", "value": n / (batch_step_ms * sim_steps / 1e3),
-        "unit": "sims/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": batch_step_ms,
+        "unit": "sims/s", "n_gpus": world, "steps": steps, "warmup": warmup, "ms_per_step": batch_step_ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"batched {n} cells R~logU[{r_range[0]:g},{r_range[1]:g}], per-cell VP materials",
                    "tets": nt,
-                   "tile_tets": info["tile_tets"], "autotune_ms_per_10_steps": info["tuning"],
+                   "tile_tets": info["tile_tets"], "buckets": info["buckets"],
+                   "autotune_ms_per_10_steps": info["tuning"],
                    "batch_tetra_steps_per_s": nt / (batch_step_ms / 1e3),
                    "looped_plain_ms_per_step": loop_step_ms,
                    "looped_plain_sims_per_s": n / (loop_step_ms * sim_steps / 1e3),
@@ -310,7 +337,82 @@ def run_batched(args):
                    "mesh_gen_s": t_mesh, "setup_s": t_setup, "status": status,
                    "cells_with_status_max_rank": n_bad, "parallelism": f"cells sharded by LPT over {world} GPU(s)"},
     }
-    print(json.dumps(line), flush=True)
+    return line
+
+
+def run_batched(args):
+    world, rank, local, dist = dist_setup()
+    line = batched_measure(args, world, rank, local, dist, args.steps, args.warmup)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+def e2e_api(w, mesh, local: int, steps: int) -> dict:
+    """The workload through the reference-facing Python surface: Simulation (built on the same
+    mesh), Substrate, a Sphere whose position is a plain Python callable (evaluated on the host
+    for every step, uploaded as a per-step table), FiniteStrainViscoplastic and VelocityVerlet,
+    and Simulation.run's output loop with file writing off: every interval reads the positions
+    back and evaluates the recorded quantities (time, indentation, indenter force). Wall clock
+    over run(), after one untimed interval that captures the step graph."""
+    import tempfile
+
+    from nofluidx3d_gb300.interactions import FiniteStrainViscoplastic, Sphere
+    from nofluidx3d_gb300.Simulation import Simulation
+    from nofluidx3d_gb300.TetraCell import TetraCell
+
+    interval = w.record_every
+    frames = max(1, steps // interval)
+    sph = w.contacts(mesh)[w.record_contact]
+    p0, v = sph["p0"], sph["v"]
+    R = w.radius
+    with tempfile.TemporaryDirectory() as td:
+        cfg = {"gpu": local, "RhoSI": 1.0, "SimulationTimeSI": float(frames * interval), "VTKFramesTotal": frames,
+               "OutputDir": td + "/", "InitialDistance": w.initial_distance(mesh), "MoveTimeSI": 1e30,
+               "VelocitySI": w.speed, "SphereRadiusSI": w.sphere_radius,
+               "CELL": {"RadiusSI": R, "RadiusSIM": R, "YoungsModulusSI": 1e-2, "PoissonRatio": 0.3}}
+        sim = Simulation(cfg, verbose=False, cell=TetraCell.from_arrays(mesh.points, mesh.tets, radius=R))
+        sim.setInteractionSubstrate()
+        sphere = Sphere(sph["radius"], lambda t: p0 - v * t, sph["k"])
+        sim.register(sphere)
+        sim.register(FiniteStrainViscoplastic(*w.vp_params()))
+        sim.setInteractionVelocityVerlet(damping=w.xi)
+        sim.recordedQuantities.append(lambda: v * sim.time)
+        sim.recordedQuantities.append(lambda: sim.handle.indenter_force(sphere.contactId))
+        sim._advance(interval)
+        sim.handle.sync()
+        t0 = time.perf_counter()
+        data = sim.run(writeStress=False, writePressure=False, write=False)
+        dt = time.perf_counter() - t0
+        status = sim.handle.status()
+        sim.close()
+    n = frames * interval
+    return {"value": mesh.num_tetra * n / dt, "unit": "tetra-steps/s", "steps": n, "interval": interval,
+            "outputs": frames + 1, "h2d_bytes_per_step": 8.0 * (interval + 1) / interval,
+            "d2h_bytes_per_step": (frames + 1) * (8.0 * 3 * mesh.num_points + 8.0) / n,
+            "path": "Simulation.run(write=False): Python sphereFunc -> position tables, positions read back "
+                    "every interval, force via the handle's readout",
+            "final_force": float(data[-1, 2]), "status": status}
+
+
+def roofline_1m(local: int, launches: int, peak: float) -> dict:
+    """The element pass on the 1M-tetra cell (R = 34 plain-large construction): algorithmic bytes
+    per launch over its average duration across back-to-back launches, after 300 steps."""
+    from nofluidx3d_gb300.core import CellSim
+
+    w = workloads.plain_large_1m()
+    mesh = w.mesh()
+    sim = CellSim(local)
+    w.configure(sim, mesh, max_rows=40)
+    sim.time_steps(300)
+    step_ms = sim.time_steps(2000) / 2000
+    ms = sim.profile_tet_pass(launches)
+    sim.close()
+    nt = mesh.num_tetra
+    achieved = ELEM_BYTES[w.material] * nt / (ms / 1e3) / 1e9
+    return {"workload": w.name, "tets": nt, "tet_pass_ms": ms, "launches_timed": launches, "achieved": achieved,
+            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "ms_per_step": step_ms,
+            "tetra_steps_per_s": nt / (step_ms / 1e3),
+            "step_frac": (ELEM_BYTES[w.material] * nt + NODE_BYTES * mesh.num_points) / (step_ms / 1e3) / 1e9 / peak}
 
 
 def main():
@@ -335,6 +437,12 @@ def main():
                     help="steps per cell when timing the looped plain path (multiples of 100 run as CUDA graphs)")
     ap.add_argument("--batch-rmin", type=float, default=6.0)
     ap.add_argument("--batch-rmax", type=float, default=40.0)
+    ap.add_argument("--batch-steps", type=int, default=200, help="timed batch steps in the default run")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched measurement of the default run")
+    ap.add_argument("--no-api", action="store_true", help="skip the Simulation-surface e2e_api measurement")
+    ap.add_argument("--no-1m", action="store_true", help="skip the 1M-tetra roofline")
+    ap.add_argument("--clock-window-s", type=float, default=2.0,
+                    help="untimed steps run just before the timed region while clocks are sampled")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -348,7 +456,9 @@ def main():
 
     w = workloads.WORKLOADS[args.workload]()
     mesh = w.mesh()
-    total = args.warmup + args.steps + args.profile_steps + args.e2e_steps + 400
+    # force rows for every step this process runs (the clock window's length depends on the step
+    # time: up to about 2 M steps for the smallest cell)
+    total = args.warmup + args.steps + args.profile_steps + args.e2e_steps + 400 + 2_000_000
     sim = CellSim(local)
     w.configure(sim, mesh, max_rows=total // w.record_every + 2)
     nt, npn = mesh.num_tetra, mesh.num_points
@@ -358,12 +468,20 @@ def main():
     sim.time_steps(args.warmup)
     if args.warmup < 100:
         sim.time_steps(100)
-    barrier(dist, local)
+    # The clock sampler (nvidia-smi, 200 ms period) runs from the start of an untimed window of at
+    # least --clock-window-s seconds of the same steps through the end of the timed region, so
+    # that a short timed region still has clock samples under load around it.
     clocks = ClockSampler(local)
     clocks.start()
+    window_ms = 0.0
+    while window_ms < 1e3 * args.clock_window_s:
+        window_ms += sim.time_steps(1000)
+    barrier(dist, local)
     ms = sim.time_steps(args.steps)
     barrier(dist, local)
     clk = clocks.stop()
+    if clk is not None:
+        clk["window"] = f"{window_ms / 1e3:.1f} s of the same steps just before the timed region, and the timed region"
     ms = reduce_max(dist, ms, local)
     value = world * nt * args.steps / (ms / 1e3)
 
@@ -416,9 +534,15 @@ def main():
     h2d = 8.0 * w.record_every * intervals / e2e_steps + 16.0 / w.record_every
     d2h = d2h_bytes / e2e_steps
     status = sim.status()
+    sim.close()
+
+    api = None if args.no_api else e2e_api(w, mesh, local, args.e2e_steps)
+    r1m = None if args.no_1m else roofline_1m(local, args.tet_launches, peaks["hbm_gbs"])
+    batched = None
+    if not args.no_batched:
+        batched = batched_measure(args, world, rank, local, dist, args.batch_steps, 50)
 
     if rank != 0:
-        sim.close()
         barrier(dist, local)
         return
     cpu = None
@@ -431,9 +555,8 @@ def main():
         "metric": METRIC, "value": value, "unit": "tetra-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": w.name, "tets": nt, "nodes": npn, "parallelism": "replicas" if world > 1 else "single",
-                   "l2": f"inputs larger than L2: {(ELEM_BYTES[w.material] * nt + NODE_BYTES * npn) / 1e6:.0f} MB "
-                         "of algorithmic state streamed per step vs 129 MB L2",
+        "config": bench_config(w, nt, npn, world),
+        "diagnostics": {
                    "step_bytes_per_tetra": ELEM_BYTES[w.material] + NODE_BYTES * npn / nt,
                    "step_gbs": (ELEM_BYTES[w.material] * nt + NODE_BYTES * npn) / (ms / args.steps / 1e3) / 1e9,
                    "tet_pass_ms": tet_launch_ms, "tet_pass_ms_bracketed": tet_avg,
@@ -446,11 +569,18 @@ def main():
         "fp32": fp32_rate(flops_per_tet, nt, tet_launch_ms, local, clk),
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_val, "unit": "tetra-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e_api": api,
+        "roofline_1m": r1m,
+        "batched": None if batched is None else {
+            "sims_per_s": batched["value"], "ms_per_step": batched["ms_per_step"], "steps": batched["steps"],
+            **{k: batched["config"][k] for k in ("workload", "tets", "buckets", "tile_tets", "batch_tetra_steps_per_s",
+                                                 "looped_plain_ms_per_step", "looped_plain_sims_per_s",
+                                                 "speedup_vs_looped_plain", "autotune_ms_per_10_steps", "status",
+                                                 "cells_with_status_max_rank", "setup_s")}},
         "gpu_launches": 2 * args.steps + (args.steps + 99) // 100,
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)
-    sim.close()
     barrier(dist, local)
 
 

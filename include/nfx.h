@@ -112,7 +112,9 @@ int nfx_add_contact(nfx_sim* sim, int kind, double k, double radius, double p0, 
 /* Supplies explicit per-step positions pos[0..n) for times t0..t0+n-1 of contact `id`,
  * overriding its schedule; times outside the table use the nearest entry. This keeps
  * arbitrary host callables working: the reference re-evaluates wallFunc(t) on the host every
- * step in beforeTimeStep (interactions/Plane.py:39-41, Sphere.py:41-43). n = 0 removes it. */
+ * step in beforeTimeStep (interactions/Plane.py:39-41, Sphere.py:41-43). n = 0 removes it.
+ * Stream-ordered: steps enqueued before the call use the previous table, later ones this one;
+ * the call does not wait for the enqueued steps, and pos may be reused when it returns. */
 int nfx_set_contact_table(nfx_sim* sim, int id, int64_t t0, int64_t n, const double* pos);
 
 /* Velocity Verlet settings: damping xi (VelocityVerlet.cl:11 hard-codes 0.005) and the
@@ -152,6 +154,12 @@ int nfx_record_now(nfx_sim* sim);
 int nfx_snapshot(nfx_sim* sim, double* points_out, double* rows_out, int64_t max_rows, int64_t* n_rows);
 int nfx_snapshot_wait(nfx_sim* sim);
 
+/* Page-locked host memory (cudaMallocHost) for nfx_snapshot's buffers, so that callers without
+ * a CUDA runtime of their own can overlap output copies with the steps; freed by nfx_host_free.
+ * No counterpart in the reference. */
+int nfx_host_alloc(size_t bytes, void** out);
+int nfx_host_free(void* p);
+
 /* Waits for all enqueued work of the handle. */
 int nfx_sync(nfx_sim* sim);
 
@@ -179,6 +187,25 @@ int nfx_get_tet_field(nfx_sim* sim, int which, double* out);
 /* Plastic deformation tensor Fp, double[9*nt] SoA (plasticDeformationTensor layout,
  * Interactions.py:279-281). */
 int nfx_get_plastic_tensor(nfx_sim* sim, double* out);
+
+/* Overwrites the plastic deformation tensor Fp, double[9*nt] SoA in user tetra order (the
+ * plasticDeformationTensor buffer of Interactions.py:279-281 written back with writeToGPU); the
+ * accumulated plastic strain is kept. Viscoplastic material only. */
+int nfx_set_plastic_tensor(nfx_sim* sim, const double* in);
+
+/* Checkpoint of the whole simulation state, for resuming a run bit for bit: node displacements
+ * (hi and lo parts), velocities and previous forces, the viscoplastic state and stress fields,
+ * the time, the status word and the force rows recorded so far, in the library's internal
+ * order and precision. The reference's only restart reloads positions from a VTK frame
+ * (SimulationLegacy.py:103-112, initCheckPointVTK), which loses velocities, forces and plastic
+ * state. nfx_checkpoint_size gives the bytes nfx_checkpoint_save writes into a host buffer
+ * (it waits for the enqueued steps first). nfx_checkpoint_load restores them into a handle set
+ * up the same way (same mesh, material model and, when rows were saved, nfx_set_record with at
+ * least as many rows); parameters, contacts and host position tables are set-up, not state, and
+ * are not stored. */
+int nfx_checkpoint_size(nfx_sim* sim, int64_t* bytes);
+int nfx_checkpoint_save(nfx_sim* sim, void* buf, int64_t bytes);
+int nfx_checkpoint_load(nfx_sim* sim, const void* buf, int64_t bytes);
 
 /* Copies the recorded rows (3 doubles each) into rows; *n_rows receives how many rows exist
  * up to the current time (at most max_rows). */
@@ -217,14 +244,15 @@ int nfx_mesh_info(nfx_sim* sim, int64_t* ntiles, int64_t* tile_nodes);
 /* ------------------------------------------------------------------------------------------
  * Batched cells. The reference advances one cell per Simulation (nofluidx3d/Simulation.py:35);
  * a batch advances many independent cells of uneven size and material together: one element-pass
- * launch and one node-pass launch per step for all cells, captured as a CUDA graph. All cells of
+ * launch per size bucket and one node-pass launch per step for all cells, captured as a CUDA graph. All cells of
  * a batch use one material model; each has its own parameters, contacts, integrator settings and
  * force curve. Set-up calls come before nfx_batch_finalize; stepping and readback after.
  * ------------------------------------------------------------------------------------------ */
 typedef struct nfx_batch nfx_batch;
 
-/* tile_tets: 64, 128, 256 or 512 tetrahedra per tile, or 0 to let nfx_batch_finalize time a
- * representative sub-batch with 64, 128 and 256 and keep the fastest. */
+/* tile_tets: 64, 128, 256 or 512 tetrahedra per tile for every cell, or 0 to group the cells by
+ * size into buckets and let nfx_batch_finalize choose each bucket's tile size, timing a
+ * representative sub-batch of the bucket with 64, 128 and 256 and keeping the fastest. */
 int nfx_batch_create(int device, int tile_tets, nfx_batch** out);
 int nfx_batch_destroy(nfx_batch* batch);
 /* Adds a cell (layouts as nfx_set_mesh); *cell receives its index. */
@@ -260,13 +288,20 @@ int nfx_batch_indenter_force(nfx_batch* batch, int contact, double* out);
 int nfx_batch_get_curve(nfx_batch* batch, int cell, double* rows, int64_t max_rows, int64_t* n_rows);
 /* Node positions of one cell, double[3*np] SoA in the cell's user order. */
 int nfx_batch_get_points(nfx_batch* batch, int cell, double* out);
+/* Overwrites the node positions of one cell (as nfx_set_points; Bridge.writeToGPU). */
+int nfx_batch_set_points(nfx_batch* batch, int cell, const double* in);
 int nfx_batch_status(nfx_batch* batch, uint32_t* flags, int clear);
 /* The status bits of every cell, flags[cells] (the batch status is their union). */
 int nfx_batch_cell_status(nfx_batch* batch, uint32_t* flags, int clear);
 /* Cells, total tetrahedra and nodes, tile size in use. */
 int nfx_batch_info(nfx_batch* batch, int64_t* cells, int64_t* tets, int64_t* nodes, int* tile_tets);
-/* The autotuner's candidates and their times (ms for 10 steps of the sub-batch). */
+/* The autotuner's candidates and their times (ms for 10 steps of the sub-batch), bucket after
+ * bucket (three candidates per bucket). */
 int nfx_batch_tuning(nfx_batch* batch, int* tiles, float* ms, int max_n, int* n);
+/* The buckets of a finalized batch: cells are grouped by size (up to 32,768 tetra, up to 262,144,
+ * larger) when the tile size is autotuned, each bucket with its own tile size and its own
+ * element-pass launch; a fixed tile size gives one bucket. Per bucket: tile size, cells, tetra. */
+int nfx_batch_buckets(nfx_batch* batch, int max_n, int* n, int* tile_tets, int64_t* cells, int64_t* tets);
 
 /* Indenter force of one contact on node positions the caller keeps in device memory, written
  * to one double in device memory. This entry point has no counterpart in the reference.
@@ -279,8 +314,11 @@ int nfx_batch_tuning(nfx_batch* batch, int* tiles, float* ms, int max_n, int* n)
  * GPU that loads this library holds until the process exits; np is therefore limited to
  * NFX_NOALLOC_MAX_NODES, and a larger np returns NFX_ERR_ARG.
  *
- * The first call on a device looks up the array's device address with that device current;
- * make that first call before any stream capture. Every call shares the array, and it keeps
+ * Each call made outside stream capture looks up the array's device address in the current
+ * context of `device` (so a reset device or another context gets its own copy); a call inside
+ * a capture uses the address of the last uncaptured call, so make the first call on a device
+ * before any stream capture. The call makes `device` current while it runs and restores the
+ * caller's current device before it returns. Every call shares the array, and it keeps
  * the last call's contents (the counter is cleared at the start of each call): calls whose
  * work overlaps on the GPU — on different streams with no ordering between them — race and
  * give wrong results.

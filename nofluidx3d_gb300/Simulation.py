@@ -7,6 +7,9 @@ the C ABI. Output frames are legacy-VTK files; non-finite positions raise Floati
 instead of exit().
 
 `con` is a path to the reference's JSON config or an already-parsed dict with the same keys.
+`cell` optionally supplies the TetraCell directly (e.g. a generated Kuhn sphere through
+TetraCell.from_arrays) instead of reading CELL.InitVTK, which avoids a text VTK round trip for
+meshes of millions of tetrahedra.
 """
 
 from __future__ import annotations
@@ -39,7 +42,7 @@ def _linear_schedule(p0: float, v: float, tmove: float):
 
 
 class Simulation:
-    def __init__(self, con, verbose: bool = True):
+    def __init__(self, con, verbose: bool = True, cell: TetraCell | None = None):
         if isinstance(con, dict):
             self.parameters = con
         else:
@@ -64,8 +67,11 @@ class Simulation:
         self.vtkfilespath = self.parameters["OutputDir"] + "vtkfiles/frame"
         os.makedirs(self.parameters["OutputDir"] + "vtkfiles", exist_ok=True)
 
-        self.cell = TetraCell(self.parameters["CELL"]["InitVTK"], radius=self.parameters["CELL"]["RadiusSIM"],
-                              recenter=True)
+        if cell is not None:
+            self.cell = cell
+        else:
+            self.cell = TetraCell(self.parameters["CELL"]["InitVTK"], radius=self.parameters["CELL"]["RadiusSIM"],
+                                  recenter=True)
         self.numPoints = self.cell.points[:, 0].size
         self.numTetra = self.cell.tetras[:, 0].size
         self._print(f"Particle mesh consists of {self.numPoints} vertices and {self.numTetra} tetrahedrons")
@@ -224,28 +230,67 @@ class Simulation:
     def timeStep(self):
         self._advance(1)
 
-    def run(self, writeStress=True, writePressure=True, writeVolumeChange=False):
+    def run(self, writeStress=True, writePressure=True, writeVolumeChange=False, write=True):
+        """The output loop of Simulation.py:239-290, with the same frames and simdata.dat rows.
+        The device runs the next output interval while the host writes the current frame: each
+        frame's positions come from an output snapshot (nfx_snapshot into page-locked buffers),
+        and its recorded quantities and per-tetra fields are read at the frame's time before the
+        next interval is enqueued. write=False does every readback of an output but writes no
+        frame and no simdata.dat."""
+        from .core import PinnedArray
+
         self._print(f"VTKInterval: {self.VTKInterval}")
         starttimes, endtimes = [], []
         numberCycles = self.parameters["VTKFramesTotal"]
-        writeVTK(self, writeStress=writeStress, writePressure=writePressure, writeVolumeChange=writeVolumeChange)
+        writeVTK(self, writeStress=writeStress, writePressure=writePressure, writeVolumeChange=writeVolumeChange,
+                 write=write)
         dataPoints = np.array([quant() for quant in self.recordedQuantities])
-        np.savetxt(self.parameters["OutputDir"] + "simdata.dat", dataPoints)
-        for i in range(numberCycles):
+        if write:
+            np.savetxt(self.parameters["OutputDir"] + "simdata.dat", dataPoints)
+        frames = [PinnedArray(3 * self.numPoints) for _ in range(2)]
+        if numberCycles > 0:
             starttimes.append(time.time())
             self._advance(self.VTKInterval)
-            self.handle.sync()
+        for i in range(numberCycles):
+            buf = frames[i % 2].array
+            self.handle.snapshot(buf)  # positions at the end of this interval, copied asynchronously
+            frame_time = self.time
+            row = [quant() for quant in self.recordedQuantities]
+            vm = self.handle.tet_field(0) if writeStress else None
+            pr = self.handle.tet_field(1) if writePressure else None
+            if i + 1 < numberCycles:  # the next interval runs while this frame is written
+                starttimes.append(time.time())
+                self._advance(self.VTKInterval)
+            self.handle.snapshot_wait()
             anatime1 = time.time()
-            writeVTK(self, writeStress=writeStress, writePressure=writePressure, writeVolumeChange=writeVolumeChange)
-            dataPoints = np.vstack((dataPoints, [quant() for quant in self.recordedQuantities]))
-            np.savetxt(self.parameters["OutputDir"] + "simdata.dat", dataPoints)
+            writeVTK(self, writeStress=writeStress, writePressure=writePressure, writeVolumeChange=writeVolumeChange,
+                     write=write, positions=buf, time=frame_time, vonMises=vm, pressure=pr)
+            dataPoints = np.vstack((dataPoints, row))
+            if write:
+                np.savetxt(self.parameters["OutputDir"] + "simdata.dat", dataPoints)
             anatime2 = time.time()
             endtimes.append(time.time())
-            cycleTime = np.average(np.array(endtimes) - np.array(starttimes))
+            cycleTime = np.average(np.array(endtimes) - np.array(starttimes[:len(endtimes)]))
             self._print(f"| Average # of simulation steps per second: {np.round(self.VTKInterval / cycleTime, 1)} "
                         f"| VTK cycle took {np.round(anatime2 - anatime1, 1)} seconds", end="\r")
+        self.handle.sync()
         self._print("")
         return dataPoints
+
+    def saveCheckpoint(self, path: str) -> None:
+        """Write the whole device state (positions, velocities, previous forces, plastic state,
+        time, recorded force rows) to `path`; loadCheckpoint resumes from it bit for bit. The
+        reference's restart (SimulationLegacy.py:103-112) reloads positions only."""
+        data = self.handle.checkpoint()
+        with open(path, "wb") as f:
+            f.write(data)
+
+    def loadCheckpoint(self, path: str) -> None:
+        """Restore a saveCheckpoint file into this simulation, set up with the same mesh and
+        interactions (registered before the call)."""
+        with open(path, "rb") as f:
+            self.handle.restore(f.read())
+        self.time = self.handle.time
 
     def close(self):
         self.handle.close()

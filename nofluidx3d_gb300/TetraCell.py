@@ -20,9 +20,9 @@ class TetraCell:
     def __init__(self, path, radius: float = 18.0, recenter: bool = True, mesh: VtkMesh | None = None):
         self.mesh = mesh if mesh is not None else read_vtk(str(path))
         if recenter:
-            transvec = -self.mesh.points[0]  # point 0 of the reference mesh marks the origin
+            transvec = -self.mesh.points[0]  # the mesh's first point becomes the centre
             self.mesh.translate(transvec, inplace=True)
-            radius_mesh = np.abs(self.mesh.points[1][0])  # x-value of point 1
+            radius_mesh = np.abs(self.mesh.points[1][0])  # the second point lies on the x axis at the radius
             self.mesh.scale(radius / radius_mesh, inplace=True)
         self.points = self.mesh.points
         self.radius = radius

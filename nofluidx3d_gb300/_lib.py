@@ -62,6 +62,10 @@ _SIGS = {
     "nfx_set_force_old": ([_vp, _vp], C.c_int),
     "nfx_get_tet_field": ([_vp, C.c_int, _vp], C.c_int),
     "nfx_get_plastic_tensor": ([_vp, _vp], C.c_int),
+    "nfx_set_plastic_tensor": ([_vp, _vp], C.c_int),
+    "nfx_checkpoint_size": ([_vp, C.POINTER(_i64)], C.c_int),
+    "nfx_checkpoint_save": ([_vp, _vp, _i64], C.c_int),
+    "nfx_checkpoint_load": ([_vp, _vp, _i64], C.c_int),
     "nfx_get_curve": ([_vp, _vp, _i64, C.POINTER(_i64)], C.c_int),
     "nfx_indenter_force": ([_vp, C.c_int, C.POINTER(C.c_double)], C.c_int),
     "nfx_status": ([_vp, C.POINTER(C.c_uint32), C.c_int], C.c_int),
@@ -71,6 +75,8 @@ _SIGS = {
     "nfx_mesh_info": ([_vp, C.POINTER(_i64), C.POINTER(_i64)], C.c_int),
     "nfx_snapshot": ([_vp, _vp, _vp, _i64, C.POINTER(_i64)], C.c_int),
     "nfx_snapshot_wait": ([_vp], C.c_int),
+    "nfx_host_alloc": ([C.c_size_t, C.POINTER(_vp)], C.c_int),
+    "nfx_host_free": ([_vp], C.c_int),
     "nfx_divide_check": ([C.c_int, _i64, _vp, _vp, _vp], C.c_int),
     "nfx_indenter_force_noalloc": ([C.c_int, _i64, _vp, C.c_int, C.c_double, C.c_double, C.c_double, _vp, _vp],
                                    C.c_int),
@@ -92,10 +98,12 @@ _SIGS = {
     "nfx_batch_indenter_force": ([_vp, C.c_int, _vp], C.c_int),
     "nfx_batch_get_curve": ([_vp, C.c_int, _vp, _i64, C.POINTER(_i64)], C.c_int),
     "nfx_batch_get_points": ([_vp, C.c_int, _vp], C.c_int),
+    "nfx_batch_set_points": ([_vp, C.c_int, _vp], C.c_int),
     "nfx_batch_status": ([_vp, C.POINTER(C.c_uint32), C.c_int], C.c_int),
     "nfx_batch_cell_status": ([_vp, _vp, C.c_int], C.c_int),
     "nfx_batch_info": ([_vp, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64), C.POINTER(C.c_int)], C.c_int),
     "nfx_batch_tuning": ([_vp, _vp, _vp, C.c_int, C.POINTER(C.c_int)], C.c_int),
+    "nfx_batch_buckets": ([_vp, C.c_int, C.POINTER(C.c_int), _vp, _vp, _vp], C.c_int),
     "nfx_mlp_create": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _i64, C.POINTER(_vp)], C.c_int),
     "nfx_mlp_destroy": ([_vp], C.c_int),
     "nfx_mlp_num_params": ([_vp, C.POINTER(_i64)], C.c_int),

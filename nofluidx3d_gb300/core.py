@@ -36,6 +36,27 @@ def _ptr(a: np.ndarray) -> int:
     return a.ctypes.data
 
 
+class PinnedArray:
+    """A float64 numpy array in page-locked host memory (nfx_host_alloc), for output snapshots
+    whose copies overlap the steps; the memory is freed with the object."""
+
+    def __init__(self, n: int):
+        self._L = _lib.load()
+        p = C.c_void_p()
+        check(self._L.nfx_host_alloc(8 * max(int(n), 1), C.byref(p)))
+        self._p = p
+        self.array = np.ctypeslib.as_array(C.cast(p, C.POINTER(C.c_double)), shape=(max(int(n), 1),))[:int(n)]
+
+    def __del__(self):
+        try:
+            if getattr(self, "_p", None) is not None and self._p.value:
+                self.array = None
+                self._L.nfx_host_free(self._p)
+                self._p = None
+        except Exception:
+            pass
+
+
 class CellSim:
     """One cell simulation on a CUDA device (see include/nfx.h for the semantics of each call)."""
 
@@ -192,6 +213,26 @@ class CellSim:
         check(self._L.nfx_get_plastic_tensor(self._h, _ptr(out)))
         return out
 
+    def set_plastic_tensor_soa(self, fp: np.ndarray) -> None:
+        """Overwrite Fp (SoA 9*nt doubles, user tetra order); the plastic strain is kept."""
+        a = np.ascontiguousarray(fp, np.float64)
+        if a.size != 9 * self.nt:
+            raise ValueError("9*nt values expected")
+        check(self._L.nfx_set_plastic_tensor(self._h, _ptr(a)))
+
+    def checkpoint(self) -> bytes:
+        """The whole state (after the enqueued steps) as an opaque byte string for restore()."""
+        n = C.c_int64()
+        check(self._L.nfx_checkpoint_size(self._h, C.byref(n)))
+        buf = np.empty(n.value, np.uint8)
+        check(self._L.nfx_checkpoint_save(self._h, _ptr(buf), n.value))
+        return buf.tobytes()
+
+    def restore(self, data: bytes) -> None:
+        """Restore a checkpoint() into a handle set up with the same mesh and material model."""
+        buf = np.frombuffer(data, np.uint8)
+        check(self._L.nfx_checkpoint_load(self._h, buf.ctypes.data, buf.size))
+
     def curve(self, max_rows: int = 1 << 20) -> np.ndarray:
         n = C.c_int64()
         check(self._L.nfx_get_curve(self._h, None, 0, C.byref(n)))
@@ -333,6 +374,13 @@ class Batch:
         check(self._L.nfx_batch_get_points(self._h, int(cell), _ptr(out)))
         return from_soa(out, 3)
 
+    def set_points(self, cell: int, pts: np.ndarray) -> None:
+        """Overwrite the node positions of one cell ((np, 3) or SoA 3*np doubles)."""
+        a = to_soa(pts) if np.asarray(pts).ndim == 2 else np.ascontiguousarray(pts, np.float64)
+        if a.size != 3 * self.cells[cell][0]:
+            raise ValueError("3*np positions expected")
+        check(self._L.nfx_batch_set_points(self._h, int(cell), _ptr(a)))
+
     def status(self, clear: bool = False) -> int:
         f = C.c_uint32()
         check(self._L.nfx_batch_status(self._h, C.byref(f), int(bool(clear))))
@@ -341,9 +389,16 @@ class Batch:
     def info(self) -> dict:
         a, b, c, d = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int()
         check(self._L.nfx_batch_info(self._h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))
-        tiles = (C.c_int * 8)()
-        ms = (C.c_float * 8)()
+        tiles = (C.c_int * 9)()
+        ms = (C.c_float * 9)()
         n = C.c_int()
-        check(self._L.nfx_batch_tuning(self._h, C.cast(tiles, C.c_void_p), C.cast(ms, C.c_void_p), 8, C.byref(n)))
+        check(self._L.nfx_batch_tuning(self._h, C.cast(tiles, C.c_void_p), C.cast(ms, C.c_void_p), 9, C.byref(n)))
+        nb = C.c_int()
+        bt = (C.c_int * 3)()
+        bc = (C.c_int64 * 3)()
+        bn = (C.c_int64 * 3)()
+        check(self._L.nfx_batch_buckets(self._h, 3, C.byref(nb), C.cast(bt, C.c_void_p), C.cast(bc, C.c_void_p),
+                                        C.cast(bn, C.c_void_p)))
         return {"cells": a.value, "tets": b.value, "nodes": c.value, "tile_tets": d.value,
-                "tuning": [(tiles[i], ms[i]) for i in range(n.value)]}
+                "tuning": [(tiles[i], ms[i]) for i in range(n.value)],
+                "buckets": [{"tile_tets": bt[i], "cells": bc[i], "tets": bn[i]} for i in range(nb.value)]}

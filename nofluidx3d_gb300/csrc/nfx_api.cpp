@@ -60,9 +60,17 @@ struct nfx_sim {
     long long record_every = 0, max_rows = 0, fields_every = 0;
     long long* d_node_user = nullptr;
     double* d_stage = nullptr;
-    double* d_tables[MAX_CONTACTS] = {nullptr, nullptr, nullptr, nullptr};
-    long long* d_meta[MAX_CONTACTS] = {nullptr, nullptr, nullptr, nullptr};
-    long long table_cap[MAX_CONTACTS] = {0, 0, 0, 0};
+    // Per-step position tables of the contacts, two buffers per contact: a new table goes into
+    // the buffer the enqueued steps do not read, and the cell table is repointed in stream order.
+    // ev_table[c][k] marks the end of the work that may read buffer k (recorded when the cell
+    // table moves away from it); a buffer is rewritten only after its event, so refilling a table
+    // never drains the step stream.
+    double* d_tables[MAX_CONTACTS][2] = {};
+    long long* d_meta[MAX_CONTACTS][2] = {};
+    long long table_cap[MAX_CONTACTS][2] = {};
+    int table_cur[MAX_CONTACTS] = {0, 0, 0, 0};
+    cudaEvent_t ev_table[MAX_CONTACTS][2] = {};
+    bool ev_table_set[MAX_CONTACTS][2] = {};
     // fixed-size control block
     unsigned* d_status = nullptr;
     StepClock* d_clock = nullptr;
@@ -226,6 +234,48 @@ void note_rows(nfx_sim* s, long long t_begin, long long t_end_inclusive) {
     if (last * every >= t_begin) s->rows_written = std::max(s->rows_written, std::min(last + 1, s->curve_rows));
 }
 
+// The per-node and per-tetra state a checkpoint holds, in the device's internal order: the
+// displacement hi/lo, velocity and previous force of every node and, for the viscoplastic law,
+// the plastic state and the stress fields of every tetra slot. The force accumulator is zero
+// between steps (the node pass clears it) and is not part of the state.
+struct StateArray {
+    void* ptr;
+    size_t bytes;
+};
+std::vector<StateArray> state_arrays(const nfx_sim* s) {
+    const size_t np = (size_t)s->plan.np;
+    std::vector<StateArray> a = {{s->st.ua, np * sizeof(float4)},
+                                 {s->st.ub, np * sizeof(float2)},
+                                 {s->st.va, np * sizeof(float4)},
+                                 {s->st.vb, np * sizeof(float2)}};
+    if (s->cell.mat.model == MODEL_VP && s->st.vp_a) {
+        const size_t ntp = (size_t)s->plan.nslots + ARRAY_PAD;
+        a.push_back({s->st.vp_a, ntp * sizeof(float4)});
+        a.push_back({s->st.vp_b, ntp * sizeof(float4)});
+        a.push_back({s->st.vp_c, ntp * sizeof(float2)});
+        a.push_back({s->st.fields, ntp * sizeof(float2)});
+    }
+    return a;
+}
+
+constexpr uint64_t CKPT_MAGIC = 0x3130544b43584e46ull;  // "NFXCKT01" little-endian
+struct CkptHeader {
+    uint64_t magic;
+    int64_t np, nt, nslots;
+    int32_t tile_tets, model;
+    int64_t time, rows;   // simulation time, force-curve rows stored after the state
+    uint32_t status, n_arrays;
+    uint64_t state_bytes;  // bytes of the state arrays (after the header)
+};
+
+int64_t checkpoint_bytes(const nfx_sim* s, int64_t* rows_out) {
+    uint64_t b = sizeof(CkptHeader);
+    for (const StateArray& a : state_arrays(s)) b += a.bytes;
+    const int64_t rows = s->cell.record_contact >= 0 ? std::min<long long>(s->rows_written, s->curve_rows) : 0;
+    if (rows_out) *rows_out = rows;
+    return (int64_t)(b + 3 * sizeof(double) * (uint64_t)rows);
+}
+
 }  // namespace
 
 extern "C" {
@@ -281,6 +331,15 @@ int nfx_plan_check(int64_t np, int64_t nt, const double* points, const uint32_t*
     }
     for (int64_t t = 0; t < nt; t++)
         if (seen[t] != 1) return bad("tetra not covered");
+    // fixed-point range: every tile that lists a node adds at most fix_max * 2^40 units per
+    // component to the node's signed 64-bit word, so (tiles per node) * fix_max * 2^40 < 2^63
+    std::vector<int64_t> tiles_of((size_t)np, 0);
+    for (int64_t b = 0; b < P.ntiles; b++)
+        for (int64_t q = 0; q < (int64_t)(P.tile_meta[b] >> 16); q++) tiles_of[P.tile_nodes[2 * (b * NM + q)]]++;
+    const int64_t busiest = *std::max_element(tiles_of.begin(), tiles_of.end());
+    if (busiest != P.max_tiles_per_node) return bad("tiles per node");
+    if (!((double)busiest * (double)P.fix_max * (double)FORCE_FIX_SCALE < 9223372036854775808.0))
+        return bad("fixed-point bound can overflow a node's accumulator");
     *ntiles = P.ntiles;
     *node_entries = entries;
     return NFX_OK;
@@ -346,10 +405,12 @@ int nfx_destroy(nfx_sim* s) {
     if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
     if (s->ev_snap) cudaEventDestroy(s->ev_snap);
     if (s->ev_copy) cudaEventDestroy(s->ev_copy);
-    for (int c = 0; c < MAX_CONTACTS; c++) {
-        if (s->d_tables[c]) cudaFree(s->d_tables[c]);
-        if (s->d_meta[c]) cudaFree(s->d_meta[c]);
-    }
+    for (int c = 0; c < MAX_CONTACTS; c++)
+        for (int k = 0; k < 2; k++) {
+            if (s->d_tables[c][k]) cudaFree(s->d_tables[c][k]);
+            if (s->d_meta[c][k]) cudaFree(s->d_meta[c][k]);
+            if (s->ev_table[c][k]) cudaEventDestroy(s->ev_table[c][k]);
+        }
     if (s->d_curve) cudaFree(s->d_curve);
     if (s->d_status) cudaFree(s->d_status);
     if (s->d_clock) cudaFree(s->d_clock);
@@ -376,7 +437,8 @@ int nfx_set_mesh(nfx_sim* s, int64_t np, int64_t nt, const double* points, const
     const MeshPlan& P = s->plan;
     auto& A = s->mesh_allocs;
     int* tb; int* nbg; unsigned* tm; uint2* tn; uchar4* lc; ushort4* ti; float4 *da, *db; float2* dc;
-    float4 *xh, *xl, *uh, *ul, *v, *fo; unsigned long long* fa; double* part; double* tpart;
+    float4 *xh, *xl, *ua, *va, *bbox; float2 *ub, *vb; unsigned long long* fa; double* part; double* tpart;
+    const size_t nblk = (size_t)((np + NODE_BLOCK - 1) / NODE_BLOCK);
     const int64_t ns = P.nslots;
     const size_t ntp = (size_t)ns + ARRAY_PAD;  // per-slot arrays carry ARRAY_PAD zeroed elements
     if ((rc = dalloc(s, &tb, P.tile_tet_begin.size(), &A)) || (rc = dalloc(s, &nbg, P.tile_node_begin.size(), &A)) ||
@@ -384,10 +446,10 @@ int nfx_set_mesh(nfx_sim* s, int64_t np, int64_t nt, const double* points, const
         (rc = dalloc(s, &tn, P.tile_nodes.size() / 2 + ARRAY_PAD, &A)) || (rc = dalloc(s, &lc, ntp, &A)) ||
         (rc = dalloc(s, &ti, ntp, &A)) ||
         (rc = dalloc(s, &da, ntp, &A)) || (rc = dalloc(s, &db, ntp, &A)) || (rc = dalloc(s, &dc, ntp, &A)) ||
-        (rc = dalloc(s, &xh, (size_t)np, &A)) || (rc = dalloc(s, &xl, (size_t)np, &A)) || (rc = dalloc(s, &uh, (size_t)np, &A)) ||
-        (rc = dalloc(s, &ul, (size_t)np, &A)) || (rc = dalloc(s, &v, (size_t)np, &A)) || (rc = dalloc(s, &fo, (size_t)np, &A)) ||
+        (rc = dalloc(s, &xh, (size_t)np, &A)) || (rc = dalloc(s, &xl, (size_t)np, &A)) || (rc = dalloc(s, &ua, (size_t)np, &A)) ||
+        (rc = dalloc(s, &ub, (size_t)np, &A)) || (rc = dalloc(s, &va, (size_t)np, &A)) || (rc = dalloc(s, &vb, (size_t)np, &A)) ||
         (rc = dalloc(s, &fa, 3 * (size_t)np, &A)) || (rc = dalloc(s, &part, (size_t)((np + NODE_BLOCK - 1) / NODE_BLOCK), &A)) ||
-        (rc = dalloc(s, &tpart, (size_t)P.ntiles, &A)) ||
+        (rc = dalloc(s, &tpart, (size_t)P.ntiles, &A)) || (rc = dalloc(s, &bbox, 2 * nblk, &A)) ||
         (rc = dalloc(s, &s->d_node_user, (size_t)np, &A)) || (rc = dalloc(s, &s->d_stage, 9 * (size_t)std::max(np, ns), &A))) {
         free_mesh(s);
         return rc;
@@ -421,8 +483,10 @@ int nfx_set_mesh(nfx_sim* s, int64_t np, int64_t nt, const double* points, const
     CUDA_TRY(cudaMemcpyAsync(dc, c.data(), c.size() * sizeof(float), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(xh, P.Xh.data(), P.Xh.size() * sizeof(float), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(xl, P.Xl.data(), P.Xl.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(bbox, P.block_box.data(), P.block_box.size() * sizeof(float), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(s->d_node_user, nu.data(), nu.size() * sizeof(long long), cudaMemcpyHostToDevice, st));
-    for (float4* z : {uh, ul, v, fo}) CUDA_TRY(cudaMemsetAsync(z, 0, (size_t)np * sizeof(float4), st));
+    for (float4* z : {ua, va}) CUDA_TRY(cudaMemsetAsync(z, 0, (size_t)np * sizeof(float4), st));
+    for (float2* z : {ub, vb}) CUDA_TRY(cudaMemsetAsync(z, 0, (size_t)np * sizeof(float2), st));
     CUDA_TRY(cudaMemsetAsync(fa, 0, 3 * (size_t)np * sizeof(unsigned long long), st));
     CUDA_TRY(cudaMemsetAsync(s->d_clock, 0, sizeof(StepClock), st));
     CUDA_TRY(launch_advance_time(s->st, 0, s->fields_every, s->record_every, st));
@@ -443,10 +507,12 @@ int nfx_set_mesh(nfx_sim* s, int64_t np, int64_t nt, const double* points, const
     s->mesh.dmi_c = dc;
     s->mesh.Xh = xh;
     s->mesh.Xl = xl;
-    s->st.uh = uh;
-    s->st.ul = ul;
-    s->st.v = v;
-    s->st.fo = fo;
+    s->mesh.fix_max = P.fix_max;
+    s->mesh.block_box = bbox;
+    s->st.ua = ua;
+    s->st.ub = ub;
+    s->st.va = va;
+    s->st.vb = vb;
     s->st.facc = fa;
     s->st.partials = part;
     s->st.tile_partials = tpart;
@@ -533,8 +599,11 @@ int nfx_add_contact(nfx_sim* s, int kind, double k, double radius, double p0, do
     int rc;
     if ((rc = set_device(s)) != NFX_OK) return rc;
     const int i = s->cell.n_contacts;
-    if (!s->d_meta[i] && (rc = dalloc(s, &s->d_meta[i], 2, nullptr)) != NFX_OK) return rc;
-    CUDA_TRY(cudaMemsetAsync(s->d_meta[i], 0, 2 * sizeof(long long), s->stream));
+    for (int k = 0; k < 2; k++) {
+        if (!s->d_meta[i][k] && (rc = dalloc(s, &s->d_meta[i][k], 2, nullptr)) != NFX_OK) return rc;
+        CUDA_TRY(cudaMemsetAsync(s->d_meta[i][k], 0, 2 * sizeof(long long), s->stream));
+    }
+    s->table_cur[i] = 0;
     ContactDev c{};
     c.kind = kind;
     c.k = k;
@@ -542,8 +611,8 @@ int nfx_add_contact(nfx_sim* s, int kind, double k, double radius, double p0, do
     c.p0 = p0;
     c.v = v;
     c.tmove = tmove;
-    c.table = s->d_tables[i];
-    c.meta = s->d_meta[i];
+    c.table = s->d_tables[i][0];
+    c.meta = s->d_meta[i][0];
     s->cell.c[i] = c;
     s->cell.n_contacts++;
     if (kind == NFX_CONTACT_SPHERE_INTEGRAL) {
@@ -562,24 +631,36 @@ int nfx_set_contact_table(nfx_sim* s, int id, int64_t t0, int64_t n, const doubl
     for (int64_t k = 0; k < n; k++) CHECK_ARG(std::isfinite(pos[k]), "non-finite table position");
     int rc;
     if ((rc = set_device(s)) != NFX_OK) return rc;
-    // steps already enqueued may still read the table: wait, then refill in stream order
-    CUDA_TRY(cudaStreamSynchronize(s->stream));
-    if (n > s->table_cap[id]) {
-        if (s->d_tables[id]) cudaFree(s->d_tables[id]);
-        s->d_tables[id] = nullptr;
-        s->table_cap[id] = 0;
+    // fill the buffer the enqueued steps do not read, once the work that last read it is done
+    const int cur = s->table_cur[id], nxt = 1 - cur;
+    if (s->ev_table_set[id][nxt]) CUDA_TRY(cudaEventSynchronize(s->ev_table[id][nxt]));
+    if (n > s->table_cap[id][nxt]) {
+        if (s->d_tables[id][nxt]) cudaFree(s->d_tables[id][nxt]);
+        s->d_tables[id][nxt] = nullptr;
+        s->table_cap[id][nxt] = 0;
         const long long cap = std::max<long long>(n, 4096);
-        if ((rc = dalloc(s, &s->d_tables[id], (size_t)cap, nullptr)) != NFX_OK) return rc;
-        s->table_cap[id] = cap;
-        s->cell.c[id].table = s->d_tables[id];
-        s->cell_dirty = true;
-        if ((rc = upload_cell(s)) != NFX_OK) return rc;
+        if ((rc = dalloc(s, &s->d_tables[id][nxt], (size_t)cap, nullptr)) != NFX_OK) return rc;
+        s->table_cap[id][nxt] = cap;
     }
     const long long meta[2] = {(long long)t0, (long long)n};
-    if (n > 0) CUDA_TRY(cudaMemcpyAsync(s->d_tables[id], pos, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, s->stream));
-    CUDA_TRY(cudaMemcpyAsync(s->d_meta[id], meta, sizeof(meta), cudaMemcpyHostToDevice, s->stream));
-    CUDA_TRY(cudaStreamSynchronize(s->stream));
-    return NFX_OK;
+    // Copies from pageable memory have taken the bytes when they return and run in stream order;
+    // the positions go through a pageable copy so that the caller may reuse its array at once even
+    // when it is page-locked.
+    if (n > 0) {
+        const std::vector<double> staged(pos, pos + n);
+        CUDA_TRY(cudaMemcpyAsync(s->d_tables[id][nxt], staged.data(), (size_t)n * sizeof(double),
+                                 cudaMemcpyHostToDevice, s->stream));
+    }
+    CUDA_TRY(cudaMemcpyAsync(s->d_meta[id][nxt], meta, sizeof(meta), cudaMemcpyHostToDevice, s->stream));
+    // later steps read the new buffer; everything enqueued so far may still read the old one
+    if (!s->ev_table[id][cur]) CUDA_TRY(cudaEventCreateWithFlags(&s->ev_table[id][cur], cudaEventDisableTiming));
+    CUDA_TRY(cudaEventRecord(s->ev_table[id][cur], s->stream));
+    s->ev_table_set[id][cur] = true;
+    s->cell.c[id].table = s->d_tables[id][nxt];
+    s->cell.c[id].meta = s->d_meta[id][nxt];
+    s->table_cur[id] = nxt;
+    s->cell_dirty = true;
+    return upload_cell(s);
 }
 
 int nfx_set_integrator(nfx_sim* s, double xi, int fix_top_bottom) {
@@ -642,6 +723,7 @@ int nfx_set_record(nfx_sim* s, int contact, int64_t every, int64_t max_rows) {
 }
 
 int nfx_step(nfx_sim* s, int64_t nsteps) {
+    const NvtxRange range("nfx_step");
     int rc;
     if ((rc = require_ready(s)) != NFX_OK) return rc;
     CHECK_ARG(nsteps >= 0, "negative step count");
@@ -669,6 +751,18 @@ int nfx_record_now(nfx_sim* s) {
     CUDA_TRY(prepare_readout(s, s->cell.record_contact));
     CUDA_TRY(launch_nodes(s, 0, NODE_READOUT_ROW, -1));
     note_rows(s, s->time, s->time);
+    return NFX_OK;
+}
+
+int nfx_host_alloc(size_t bytes, void** out) {
+    CHECK_ARG(out, "null argument");
+    *out = nullptr;
+    CUDA_TRY(cudaMallocHost(out, std::max<size_t>(bytes, 1)));
+    return NFX_OK;
+}
+
+int nfx_host_free(void* p) {
+    if (p) CUDA_TRY(cudaFreeHost(p));
     return NFX_OK;
 }
 
@@ -708,32 +802,33 @@ int nfx_set_points(nfx_sim* s, const double* in) {
     return NFX_OK;
 }
 
-static int get_vec(nfx_sim* s, float4* a, double* out) {
+// part 0: the velocity, part 1: the previous force (va/vb)
+static int get_vec(nfx_sim* s, int part, double* out) {
     CHECK_ARG(s && out, "null argument");
     if (!s->have_mesh) return fail(NFX_ERR_STATE, "no mesh");
     int rc;
     if ((rc = set_device(s)) != NFX_OK) return rc;
-    CUDA_TRY(launch_vec_to_user(s->mesh, a, s->d_node_user, s->d_stage, s->stream));
+    CUDA_TRY(launch_vec_to_user(s->mesh, s->st.va, s->st.vb, part, s->d_node_user, s->d_stage, s->stream));
     CUDA_TRY(cudaMemcpyAsync(out, s->d_stage, 3 * (size_t)s->plan.np * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     return NFX_OK;
 }
 
-static int set_vec(nfx_sim* s, float4* a, const double* in) {
+static int set_vec(nfx_sim* s, int part, const double* in) {
     CHECK_ARG(s && in, "null argument");
     if (!s->have_mesh) return fail(NFX_ERR_STATE, "no mesh");
     int rc;
     if ((rc = set_device(s)) != NFX_OK) return rc;
     CUDA_TRY(cudaMemcpyAsync(s->d_stage, in, 3 * (size_t)s->plan.np * sizeof(double), cudaMemcpyHostToDevice, s->stream));
-    CUDA_TRY(launch_vec_from_user(s->mesh, a, s->d_node_user, s->d_stage, s->stream));
+    CUDA_TRY(launch_vec_from_user(s->mesh, s->st.va, s->st.vb, part, s->d_node_user, s->d_stage, s->stream));
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     return NFX_OK;
 }
 
-int nfx_get_velocities(nfx_sim* s, double* out) { return s ? get_vec(s, s->st.v, out) : fail(NFX_ERR_ARG, "null handle"); }
-int nfx_set_velocities(nfx_sim* s, const double* in) { return s ? set_vec(s, s->st.v, in) : fail(NFX_ERR_ARG, "null handle"); }
-int nfx_get_force_old(nfx_sim* s, double* out) { return s ? get_vec(s, s->st.fo, out) : fail(NFX_ERR_ARG, "null handle"); }
-int nfx_set_force_old(nfx_sim* s, const double* in) { return s ? set_vec(s, s->st.fo, in) : fail(NFX_ERR_ARG, "null handle"); }
+int nfx_get_velocities(nfx_sim* s, double* out) { return s ? get_vec(s, 0, out) : fail(NFX_ERR_ARG, "null handle"); }
+int nfx_set_velocities(nfx_sim* s, const double* in) { return s ? set_vec(s, 0, in) : fail(NFX_ERR_ARG, "null handle"); }
+int nfx_get_force_old(nfx_sim* s, double* out) { return s ? get_vec(s, 1, out) : fail(NFX_ERR_ARG, "null handle"); }
+int nfx_set_force_old(nfx_sim* s, const double* in) { return s ? set_vec(s, 1, in) : fail(NFX_ERR_ARG, "null handle"); }
 
 int nfx_get_tet_field(nfx_sim* s, int which, double* out) {
     CHECK_ARG(s && out, "null argument");
@@ -1002,6 +1097,120 @@ int nfx_divide_check(int device, int64_t n, const float* a, const float* b, floa
     if (e == cudaSuccess) e = cudaMemcpy(q, d + 2 * n, bytes, cudaMemcpyDeviceToHost);
     cudaFree(d);
     if (e != cudaSuccess) return fail(NFX_ERR_CUDA, std::string("divide_check: ") + cudaGetErrorString(e));
+    return NFX_OK;
+}
+
+int nfx_checkpoint_size(nfx_sim* s, int64_t* bytes) {
+    int rc;
+    if ((rc = require_ready(s)) != NFX_OK) return rc;
+    CHECK_ARG(bytes, "null argument");
+    *bytes = checkpoint_bytes(s, nullptr);
+    return NFX_OK;
+}
+
+int nfx_checkpoint_save(nfx_sim* s, void* buf, int64_t bytes) {
+    int rc;
+    if ((rc = require_ready(s)) != NFX_OK) return rc;
+    CHECK_ARG(buf, "null buffer");
+    int64_t rows = 0;
+    const int64_t need = checkpoint_bytes(s, &rows);
+    CHECK_ARG(bytes >= need, "checkpoint buffer too small: " + std::to_string((long long)need) + " bytes needed");
+    if ((rc = set_device(s)) != NFX_OK) return rc;
+    CUDA_TRY(cudaStreamSynchronize(s->stream));  // every enqueued step has finished
+    snapshot_drain(s);
+    const std::vector<StateArray> arrays = state_arrays(s);
+    CkptHeader h{};
+    h.magic = CKPT_MAGIC;
+    h.np = s->plan.np;
+    h.nt = s->plan.nt;
+    h.nslots = s->plan.nslots;
+    h.tile_tets = s->plan.tile_tets;
+    h.model = s->cell.mat.model;
+    h.time = s->time;
+    h.rows = rows;
+    h.n_arrays = (uint32_t)arrays.size();
+    unsigned status = 0;
+    CUDA_TRY(cudaMemcpyAsync(&status, s->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, s->stream));
+    char* p = static_cast<char*>(buf) + sizeof(CkptHeader);
+    for (const StateArray& a : arrays) {
+        CUDA_TRY(cudaMemcpyAsync(p, a.ptr, a.bytes, cudaMemcpyDeviceToHost, s->stream));
+        p += a.bytes;
+        h.state_bytes += a.bytes;
+    }
+    if (rows > 0) CUDA_TRY(cudaMemcpyAsync(p, s->d_curve, 3 * sizeof(double) * (size_t)rows, cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    h.status = status;
+    std::memcpy(buf, &h, sizeof(h));
+    return NFX_OK;
+}
+
+int nfx_checkpoint_load(nfx_sim* s, const void* buf, int64_t bytes) {
+    int rc;
+    if ((rc = require_ready(s)) != NFX_OK) return rc;
+    CHECK_ARG(buf && bytes >= (int64_t)sizeof(CkptHeader), "checkpoint buffer too small");
+    CkptHeader h;
+    std::memcpy(&h, buf, sizeof(h));
+    CHECK_ARG(h.magic == CKPT_MAGIC, "not a checkpoint of this library");
+    CHECK_ARG(h.np == s->plan.np && h.nt == s->plan.nt && h.nslots == s->plan.nslots &&
+                  h.tile_tets == s->plan.tile_tets,
+              "checkpoint of a different mesh or tile size");
+    CHECK_ARG(h.model == s->cell.mat.model, "checkpoint of a different material model");
+    const std::vector<StateArray> arrays = state_arrays(s);
+    uint64_t state_bytes = 0;
+    for (const StateArray& a : arrays) state_bytes += a.bytes;
+    CHECK_ARG(h.n_arrays == arrays.size() && h.state_bytes == state_bytes, "checkpoint state layout differs");
+    CHECK_ARG(h.rows >= 0 && (uint64_t)bytes >= sizeof(CkptHeader) + state_bytes + 3 * sizeof(double) * (uint64_t)h.rows,
+              "checkpoint truncated");
+    CHECK_ARG(h.rows == 0 || (s->cell.record_contact >= 0 && h.rows <= s->curve_rows),
+              "the checkpoint holds force rows: call nfx_set_record with at least as many rows first");
+    CHECK_ARG(h.time >= 0, "negative checkpoint time");
+    if ((rc = set_device(s)) != NFX_OK) return rc;
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    snapshot_drain(s);
+    const char* p = static_cast<const char*>(buf) + sizeof(CkptHeader);
+    for (const StateArray& a : arrays) {
+        CUDA_TRY(cudaMemcpyAsync(a.ptr, p, a.bytes, cudaMemcpyHostToDevice, s->stream));
+        p += a.bytes;
+    }
+    if (h.rows > 0) CUDA_TRY(cudaMemcpyAsync(s->d_curve, p, 3 * sizeof(double) * (size_t)h.rows, cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(cudaMemsetAsync(s->st.facc, 0, 3 * (size_t)s->plan.np * sizeof(unsigned long long), s->stream));
+    CUDA_TRY(cudaMemcpyAsync(s->d_status, &h.status, sizeof(unsigned), cudaMemcpyHostToDevice, s->stream));
+    const long long t = h.time;
+    CUDA_TRY(cudaMemcpyAsync(&s->d_clock->time, &t, sizeof(long long), cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(launch_advance_time(s->st, 0, s->fields_every, s->record_every, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    s->time = t;
+    s->rows_written = h.rows;
+    return NFX_OK;
+}
+
+int nfx_set_plastic_tensor(nfx_sim* s, const double* in) {
+    CHECK_ARG(s && in, "null argument");
+    if (!s->have_mesh) return fail(NFX_ERR_STATE, "no mesh");
+    if (s->cell.mat.model != MODEL_VP || !s->st.vp_a)
+        return fail(NFX_ERR_STATE, "no viscoplastic material: call nfx_set_viscoplastic first");
+    const int64_t nt = s->plan.nt, ns = s->plan.nslots;
+    for (int64_t i = 0; i < 9 * nt; i++) CHECK_ARG(std::isfinite(in[i]), "non-finite plastic tensor entry");
+    int rc;
+    if ((rc = set_device(s)) != NFX_OK) return rc;
+    // keep the accumulated strain, replace P = Fp - I
+    std::vector<float> a(4 * (size_t)ns, 0.f), b(4 * (size_t)ns, 0.f), c(2 * (size_t)ns, 0.f);
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    CUDA_TRY(cudaMemcpyAsync(c.data(), s->st.vp_c, (size_t)ns * sizeof(float2), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    for (int64_t t = 0; t < ns; t++) {
+        const int64_t u = s->plan.tet_user[t];
+        if (u < 0) continue;
+        float P[9];
+        for (int k = 0; k < 9; k++) P[k] = (float)(in[k * nt + u] - ((k % 4 == 0) ? 1.0 : 0.0));
+        for (int k = 0; k < 4; k++) a[4 * t + k] = P[k];
+        for (int k = 0; k < 4; k++) b[4 * t + k] = P[4 + k];
+        c[2 * t] = P[8];
+    }
+    CUDA_TRY(cudaMemcpyAsync(s->st.vp_a, a.data(), (size_t)ns * sizeof(float4), cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(cudaMemcpyAsync(s->st.vp_b, b.data(), (size_t)ns * sizeof(float4), cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(cudaMemcpyAsync(s->st.vp_c, c.data(), (size_t)ns * sizeof(float2), cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));  // the host vectors go out of scope
     return NFX_OK;
 }
 

@@ -2,6 +2,7 @@
 // kernels (nfx_kernels.cu). Not part of the C ABI.
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstdint>
 #include <string>
@@ -26,7 +27,18 @@ constexpr int NODE_BLOCK = 256;
 // Fixed-point scale of the force accumulator: 2^40 (resolution 9.1e-13, range +-8.4e6).
 constexpr float FORCE_FIX_SCALE = 1099511627776.0f;
 constexpr float FORCE_FIX_INV = 1.0f / 1099511627776.0f;
-constexpr float FORCE_FIX_MAX = 4.0e6f;  // larger tile sums raise STATUS_NONFINITE
+// A node's accumulator word receives one fixed-point tile sum from every tile that lists the
+// node, so the per-tile bound is the word's range (2^63 units = 8,388,608 force units) shared
+// out over the most tiles any node of the mesh appears in: FORCE_FIX_BUDGET / max tiles (never
+// above FORCE_FIX_MAX). A tile sum above the bound raises STATUS_NONFINITE instead of being
+// added, so no sum of in-bound tile sums can wrap the 64-bit word.
+constexpr float FORCE_FIX_BUDGET = 8.0e6f;
+constexpr float FORCE_FIX_MAX = 4.0e6f;
+// The per-tile bound of a mesh whose busiest node appears in max_tiles tiles.
+inline float force_fix_bound(int max_tiles) {
+    const float b = FORCE_FIX_BUDGET / (float)(max_tiles > 0 ? max_tiles : 1);
+    return b < FORCE_FIX_MAX ? b : FORCE_FIX_MAX;
+}
 
 // Status bits raised by the kernels (read back by nfx_status).
 constexpr unsigned STATUS_NONFINITE = 1u;   // a position or force became NaN/Inf
@@ -62,6 +74,10 @@ struct MeshPlan {
     std::vector<float> dmi;                // 12 * nslots: Dm^-1 row-major (9), V0, pad, pad
     std::vector<float> Xh, Xl;             // 4 * np: reference position hi / lo parts; Xh.w holds the
                                            // inverse lumped mass of density 1 (VelocityVerlet2)
+    std::vector<float> block_box;          // 8 per node block of NODE_BLOCK internal nodes: bounding box
+                                           // of the reference positions (lo xyz, 0, hi xyz, 0), outward-rounded
+    int max_tiles_per_node = 1;            // the most tiles that list any one node
+    float fix_max = FORCE_FIX_MAX;         // per-tile fixed-point bound, force_fix_bound(max_tiles_per_node)
 };
 
 // Builds the plan from the reference's layouts (points SoA 3*np doubles, tets SoA 4*nt).
@@ -86,6 +102,11 @@ struct MeshDev {
     const float2* dmi_c;  // Dm^-1 entry 8, V0
     const float4* Xh;  // w: inverse lumped mass at density 1
     const float4* Xl;
+    const float4* block_box;  // per node block: (lo x, y, z, -), (hi x, y, z, -) of the reference
+                              // positions, rounded outwards
+    float fix_max;     // per-tile fixed-point bound of the accumulator (force_fix_bound)
+    int tile_base;     // index of this launch's first tile in the batch-wide tile numbering
+                       // (tile_partials, CellDev::tile_begin/tile_end); 0 for a single cell
 };
 
 // Device-side step clock: the simulation time at the start of the current chunk of launches and,
@@ -100,11 +121,16 @@ struct StepClock {
     unsigned record_due[CLOCK_WINDOW / 32];  // bit k: (time + k) % record_every == 0
 };
 
+// Node state, 48 bytes per node with no padding lane: the displacement u = x - X as float
+// hi + lo parts (ua: hi x, y, z and lo x; ub: lo y, z) and the velocity and previous force (va:
+// v x, y, z and f_old x; vb: f_old y, z). The element pass gathers ua/ub (24 B per tile node), the
+// node pass streams all four; the float4 + float2 split keeps every access a 16- or 8-byte
+// vector load at its natural alignment.
 struct StateDev {
-    float4* uh;     // displacement hi
-    float4* ul;     // displacement lo
-    float4* v;      // velocity
-    float4* fo;     // force of the previous step
+    float4* ua;     // displacement hi (x, y, z), displacement lo x
+    float2* ub;     // displacement lo (y, z)
+    float4* va;     // velocity (x, y, z), previous force x (previous acceleration: lumped-mass integrator)
+    float2* vb;     // previous force (y, z)
     // Element-force accumulator, 3 * np signed 64-bit fixed-point values (component d of node
     // i at [d*np + i], FORCE_FIX_SCALE units per force unit), zeroed by the node pass. Integer
     // addition is associative, so the sum does not depend on the order of the atomics.
@@ -174,6 +200,16 @@ struct BatchDev {
     long long fields_every;      // tet fields written when (t+1) % fields_every == 0
 };
 
+// An NVTX range for the lifetime of the object (a step block, a batch step, a training run), so
+// that a profiler's timeline shows the library's work by call; without an attached tool the
+// NVTX calls return at once.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
+
 // Sets the message nfx_last_error() returns on this thread (nfx_api.cpp).
 void set_error(const std::string& msg);
 
@@ -202,10 +238,12 @@ cudaError_t launch_points_to_user(const MeshDev& m, const StateDev& s, const lon
                                   cudaStream_t stream);
 cudaError_t launch_points_from_user(const MeshDev& m, const StateDev& s, const long long* node_user,
                                     const double* in, cudaStream_t stream);
-cudaError_t launch_vec_to_user(const MeshDev& m, const float4* a, const long long* node_user, double* out,
-                               cudaStream_t stream);
-cudaError_t launch_vec_from_user(const MeshDev& m, float4* a, const long long* node_user, const double* in,
-                                 cudaStream_t stream);
+// A node vector stored split over a float4 and a float2 array: part 0 is (a.x, a.y, a.z), part 1
+// is (a.w, b.x, b.y) — the velocity and the previous force of va/vb.
+cudaError_t launch_vec_to_user(const MeshDev& m, const float4* a, const float2* b, int part, const long long* node_user,
+                               double* out, cudaStream_t stream);
+cudaError_t launch_vec_from_user(const MeshDev& m, float4* a, float2* b, int part, const long long* node_user,
+                                 const double* in, cudaStream_t stream);
 cudaError_t launch_init_vp(const MeshDev& m, const StateDev& s, cudaStream_t stream);
 
 }  // namespace nfx

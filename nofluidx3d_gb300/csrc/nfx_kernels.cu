@@ -149,14 +149,15 @@ __device__ __forceinline__ float fix_to_float(unsigned long long w) {
 // the global accumulator as 64-bit fixed point, so the total does not depend on the order in
 // which tiles finish. Incidence entries are corner-force slots (corner * TILE + local tet). One
 // corner per iteration at the 56-register budget (NFX_FLUSH_UNROLL=4 takes four per iteration,
-// in the same order: faster at 64 registers, 5 % slower at 56). Returns false when the sum is out
-// of the fixed-point range (nothing is added then).
+// in the same order: faster at 64 registers, 5 % slower at 56). Returns false when a component of
+// the sum exceeds the mesh's per-tile bound fix_max (nothing is added then), which keeps every
+// node's accumulator word within its 64-bit range.
 #ifndef NFX_FLUSH_UNROLL
 #define NFX_FLUSH_UNROLL 1
 #endif
 template <int TILE>
 __device__ __forceinline__ bool node_flush(uint2 node, const unsigned short* inc, const float4* s_cf,
-                                           const StateDev& s, long long np) {
+                                           const StateDev& s, long long np, float fix_max) {
     const unsigned first = node.y >> 16, count = node.y & 0xffffu;
     if (count == 0) return true;
     const unsigned short* e = inc + first;
@@ -176,7 +177,7 @@ __device__ __forceinline__ bool node_flush(uint2 node, const unsigned short* inc
         fy += c.y;
         fz += c.z;
     }
-    if (!(fabsf(fx) <= FORCE_FIX_MAX && fabsf(fy) <= FORCE_FIX_MAX && fabsf(fz) <= FORCE_FIX_MAX)) return false;
+    if (!(fabsf(fx) <= fix_max && fabsf(fy) <= fix_max && fabsf(fz) <= fix_max)) return false;
     atomicAdd(s.facc + node.x, (unsigned long long)fix_round(fx * FORCE_FIX_SCALE));
     atomicAdd(s.facc + np + node.x, (unsigned long long)fix_round(fy * FORCE_FIX_SCALE));
     atomicAdd(s.facc + 2 * np + node.x, (unsigned long long)fix_round(fz * FORCE_FIX_SCALE));
@@ -328,7 +329,14 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * NFX_TET_REGS))
     __shared__ float4 s_xl[NMAX];
 #endif
 
-    const int b = blockIdx.x;
+    // Serpentine order across the kernel boundaries: the node pass runs its blocks in ascending
+    // node order, the element pass its tiles in descending order, so each pass starts on the nodes
+    // (accumulator words, displacements) the previous pass touched last and that are still in L2.
+    // The order changes no result: tile sums enter the accumulator as integers.
+#ifndef NFX_TILE_REVERSE
+#define NFX_TILE_REVERSE 1
+#endif
+    const int b = NFX_TILE_REVERSE ? (int)(gridDim.x - 1 - blockIdx.x) : (int)blockIdx.x;
     const int j = threadIdx.x;
     // fixed-stride tiles: the tile's slots and node entries are addressed without a load; the
     // real counts come from the tile's meta word (loaded alongside the data)
@@ -359,8 +367,10 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * NFX_TET_REGS))
     uint2 node = make_uint2(0u, 0u);
     if (j < NMAX) {
         node = __ldcs(m.tile_nodes + nb + j);
-        s_uh[j] = s.uh[node.x];
-        s_ul[j] = s.ul[node.x];
+        const float4 a = s.ua[node.x];
+        const float2 lo = s.ub[node.x];
+        s_uh[j] = a;  // the law reads x, y, z only
+        s_ul[j] = make_float4(a.w, lo.x, lo.y, 0.f);
 #if NFX_DMI_FROM_X
         s_xh[j] = m.Xh[node.x];
         s_xl[j] = m.Xl[node.x];
@@ -376,7 +386,7 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * NFX_TET_REGS))
     if (act && element_eval<MODEL, TILE>(j, t, lc, da, db, dc, pa, pb, pc, s_uh, s_ul, s_cf, s, mat, wf))
         raise_status(s, tile_cell_status(bd, b), STATUS_INVERTED);
     __syncthreads();
-    if (j < nn && !node_flush<TILE>(node, reinterpret_cast<const unsigned short*>(s_inc), s_cf, s, m.np))
+    if (j < nn && !node_flush<TILE>(node, reinterpret_cast<const unsigned short*>(s_inc), s_cf, s, m.np, m.fix_max))
         raise_status(s, tile_cell_status(bd, b), STATUS_NONFINITE);
 }
 
@@ -407,8 +417,10 @@ __global__ void __launch_bounds__(TILE) k_si_pass(MeshDev m, StateDev s, BatchDe
     uint2 node = make_uint2(0u, 0u);
     if (j < NMAX) {
         node = m.tile_nodes[b * NMAX + j];
-        s_uh[j] = s.uh[node.x];
-        s_ul[j] = s.ul[node.x];
+        const float4 a = s.ua[node.x];
+        const float2 lo = s.ub[node.x];
+        s_uh[j] = a;
+        s_ul[j] = make_float4(a.w, lo.x, lo.y, 0.f);
         s_xh[j] = m.Xh[node.x];
         s_xl[j] = m.Xl[node.x];
     }
@@ -428,11 +440,11 @@ __global__ void __launch_bounds__(TILE) k_si_pass(MeshDev m, StateDev s, BatchDe
         mode == SI_READOUT || (si == C.record_contact && clock_bit(s.clock->record_due, t_offset));
     if (want_partial) {  // uniform over the CTA
         const double tot = tile_sum<TILE>(fy, s_red);
-        if (j == 0) s.tile_partials[b] = tot;
+        if (j == 0) s.tile_partials[m.tile_base + b] = tot;
     }
     if (mode != SI_STEP) return;
     __syncthreads();
-    if (j < nn && !node_flush<TILE>(node, reinterpret_cast<const unsigned short*>(s_inc), s_cf, s, m.np))
+    if (j < nn && !node_flush<TILE>(node, reinterpret_cast<const unsigned short*>(s_inc), s_cf, s, m.np, m.fix_max))
         raise_status(s, bd.cell_status ? bd.cell_status + cell : nullptr, STATUS_NONFINITE);
 }
 
@@ -452,6 +464,30 @@ struct WallStep {
     double w;
     float wf, rf;
 };
+
+// Whether a contact can reach a node, from its node block's reference box (lo, hi: the bounding
+// box of the block's reference positions, rounded outwards) shifted by the node's own
+// displacement hi part: the coarse test of contact_force (substrate: y < w + 1e-3, plane:
+// y > w - 1e-3, sphere: within radius + 1e-3 of (0, w, 0)) applied to that box, widened by a
+// further margin that covers the float rounding of the node's coarse position x_hi + u_hi (a few
+// ulps of the coordinates) many times over. A node it rejects would fail the coarse test too, so
+// the node's reference position (16 bytes) is read only where a contact may act on the node.
+#ifndef NFX_NODE_CULL
+#define NFX_NODE_CULL 1  // 0: every node reads its reference position
+#endif
+__device__ __forceinline__ bool contact_reaches(const ContactDev& c, const WallStep& ws, float4 lo, float4 hi,
+                                                const float4& uh) {
+    if (c.kind == CONTACT_SPHERE_INTEGRAL) return false;  // a per-tetra force (element pass)
+    if (!NFX_NODE_CULL) return true;
+    const float M = 2e-3f;
+    if (c.kind == CONTACT_SUBSTRATE) return !((lo.y + uh.y) - M > ws.wf);
+    if (c.kind == CONTACT_PLANE) return !((hi.y + uh.y) + M < ws.wf);
+    const float dx = fmaxf(fmaxf(lo.x + uh.x, -(hi.x + uh.x)), 0.f);
+    const float dy = fmaxf(fmaxf((lo.y + uh.y) - ws.wf, ws.wf - (hi.y + uh.y)), 0.f);
+    const float dz = fmaxf(fmaxf(lo.z + uh.z, -(hi.z + uh.z)), 0.f);
+    const float r = ws.rf + M;
+    return !(dx * dx + dy * dy + dz * dz > r * r);
+}
 
 // The exact contact force (the reference's FP64 formulas) on one node that passed the coarse
 // float test. Every double term is formed after the low-part load, so none of the double
@@ -521,67 +557,72 @@ __device__ __forceinline__ bool contact_force(const ContactDev& c, const WallSte
 // displacement carried as hi + lo — damped velocity Verlet with unit mass and the FIXED_TOP_BOTTOM
 // pin (VelocityVerlet.cl), or the lumped-mass form (velocityVerlet2.cl) — and the accumulator reset.
 __device__ __forceinline__ double node_step(const MeshDev& m, const StateDev& s, int i, const WallStep* wall,
-                                           const CellDev& C, int rc, bool update, unsigned* cstat) {
+                                           const float4* box, const CellDev& C, int rc, bool update, unsigned* cstat) {
     const ContactDev* cs = C.c;
     const int nc = C.n_contacts;
     const long long np = m.np;
     float4 f = make_float4(fix_to_float(s.facc[i]), fix_to_float(s.facc[np + i]), fix_to_float(s.facc[2 * np + i]), 0.f);
-    const float4 xh = m.Xh[i];
-    float4 uh = s.uh[i], ul = s.ul[i];
+    const float4 a = s.ua[i];
+    const float2 lo = s.ub[i];
+    float4 uh = make_float4(a.x, a.y, a.z, 0.f), ul = make_float4(a.w, lo.x, lo.y, 0.f);
+    // the contacts that may act on this node; the reference position only where one may, or where
+    // the lumped-mass integrator needs the inverse mass (Xh.w)
+    unsigned reach = 0u;
+    const float4 blo = box[0], bhi = box[1];
+    for (int c = 0; c < nc; c++)
+        if (contact_reaches(cs[c], wall[c], blo, bhi, uh)) reach |= 1u << c;
+    float4 xh = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (reach || C.integrator == INTEGRATOR_VV2) xh = m.Xh[i];
     double fy_rc = 0.0;
     for (int c = 0; c < nc; c++) {
         double fy;
-        if (contact_force(cs[c], wall[c], xh, m.Xl + i, uh, ul, f, fy) && c == rc) fy_rc = fy;
+        if (((reach >> c) & 1u) && contact_force(cs[c], wall[c], xh, m.Xl + i, uh, ul, f, fy) && c == rc) fy_rc = fy;
     }
-    if (update && C.integrator == INTEGRATOR_VV2) {
+    if (!update) return fy_rc;
+    // velocity and previous force: streamed once per step (evict-first)
+    const float4 va = __ldcs(s.va + i);
+    const float2 vb = __ldcs(s.vb + i);
+    float3 v = make_float3(va.x, va.y, va.z);
+    float3 nf;  // the new previous-force slot
+    if (C.integrator == INTEGRATOR_VV2) {
         // velocityVerlet2.cl:9-13: v = (v + (a_old + f/m)/2) / (1 + xi/2); a = f/m - xi v;
         // x += v + a/2; the old-force slot keeps a
-        float4 v = s.v[i];
-        const float4 ao = s.fo[i];
         const float minv = xh.w * C.inv_density;
         const float c = C.vv2_c, xi = C.vv2_xi;
         const float fx = f.x * minv, fy = f.y * minv, fz = f.z * minv;
-        v.x = c * (v.x + 0.5f * (ao.x + fx));
-        v.y = c * (v.y + 0.5f * (ao.y + fy));
-        v.z = c * (v.z + 0.5f * (ao.z + fz));
+        v.x = c * (v.x + 0.5f * (va.w + fx));
+        v.y = c * (v.y + 0.5f * (vb.x + fy));
+        v.z = c * (v.z + 0.5f * (vb.y + fz));
         const float ax = fx - xi * v.x, ay = fy - xi * v.y, az = fz - xi * v.z;
         df_add(uh.x, ul.x, v.x + 0.5f * ax);
         df_add(uh.y, ul.y, v.y + 0.5f * ay);
         df_add(uh.z, ul.z, v.z + 0.5f * az);
-        if (!isfinite(uh.x + uh.y + uh.z + v.x + v.y + v.z)) raise_status(s, cstat, STATUS_NONFINITE);
-        s.uh[i] = uh;
-        s.ul[i] = ul;
-        s.v[i] = v;
-        s.fo[i] = make_float4(ax, ay, az, 0.f);
-        s.facc[i] = 0ull;
-        s.facc[np + i] = 0ull;
-        s.facc[2 * np + i] = 0ull;
-    } else if (update) {
+        nf = make_float3(ax, ay, az);
+    } else {
         const float vv_a = C.vv_a, vv_hb = C.vv_hb, vv_dm = C.vv_dm;
-        float4 v = s.v[i];
-        const float4 fo = s.fo[i];
-        v.x = vv_a * v.x + vv_hb * (f.x + fo.x);
-        v.y = vv_a * v.y + vv_hb * (f.y + fo.y);
-        v.z = vv_a * v.z + vv_hb * (f.z + fo.z);
+        v.x = vv_a * v.x + vv_hb * (f.x + va.w);
+        v.y = vv_a * v.y + vv_hb * (f.y + vb.x);
+        v.z = vv_a * v.z + vv_hb * (f.z + vb.y);
         df_add(uh.x, ul.x, vv_dm * v.x + 0.5f * f.x);
         df_add(uh.y, ul.y, vv_dm * v.y + 0.5f * f.y);
         df_add(uh.z, ul.z, vv_dm * v.z + 0.5f * f.z);
         if (i == C.fix_a || i == C.fix_b) {  // VelocityVerlet.cl:17-22: x = z = 0
-            const float4 xl = m.Xl[i];
-            uh.x = -xh.x;
+            const float4 xp = m.Xh[i], xl = m.Xl[i];
+            uh.x = -xp.x;
             ul.x = -xl.x;
-            uh.z = -xh.z;
+            uh.z = -xp.z;
             ul.z = -xl.z;
         }
-        if (!isfinite(uh.x + uh.y + uh.z + v.x + v.y + v.z)) raise_status(s, cstat, STATUS_NONFINITE);
-        s.uh[i] = uh;
-        s.ul[i] = ul;
-        s.v[i] = v;
-        s.fo[i] = make_float4(f.x, f.y, f.z, 0.f);
-        s.facc[i] = 0ull;
-        s.facc[np + i] = 0ull;
-        s.facc[2 * np + i] = 0ull;
+        nf = make_float3(f.x, f.y, f.z);
     }
+    if (!isfinite(uh.x + uh.y + uh.z + v.x + v.y + v.z)) raise_status(s, cstat, STATUS_NONFINITE);
+    s.ua[i] = make_float4(uh.x, uh.y, uh.z, ul.x);
+    s.ub[i] = make_float2(ul.y, ul.z);
+    __stcs(s.va + i, make_float4(v.x, v.y, v.z, nf.x));
+    __stcs(s.vb + i, make_float2(nf.y, nf.z));
+    s.facc[i] = 0ull;
+    s.facc[np + i] = 0ull;
+    s.facc[2 * np + i] = 0ull;
     return fy_rc;
 }
 
@@ -597,6 +638,7 @@ __global__ void __launch_bounds__(NODE_BLOCK, NFX_NODE_MIN_BLOCKS) k_node_pass(M
                                                           int readout_contact) {
     __shared__ double s_w[NODE_BLOCK / 32];
     __shared__ WallStep s_wall[MAX_CONTACTS];
+    __shared__ float4 s_box[2];
     __shared__ int s_last;
     const int cell = bd.block_cell ? __ldg(bd.block_cell + blockIdx.x) : 0;
     const CellDev& C = bd.cells[cell];
@@ -608,6 +650,7 @@ __global__ void __launch_bounds__(NODE_BLOCK, NFX_NODE_MIN_BLOCKS) k_node_pass(M
         const double w = contact_pos(C.c[threadIdx.x], t);
         s_wall[threadIdx.x] = WallStep{w, (float)w, (float)C.c[threadIdx.x].radius};
     }
+    if (threadIdx.x >= 32 && threadIdx.x < 34) s_box[threadIdx.x - 32] = m.block_box[2 * blockIdx.x + (threadIdx.x - 32)];
     __syncthreads();
     int rc;
     bool rec;
@@ -628,7 +671,7 @@ __global__ void __launch_bounds__(NODE_BLOCK, NFX_NODE_MIN_BLOCKS) k_node_pass(M
     }
     double fy = 0.0;  // y force of the readout contact on this node
     if (i < C.node_end)
-        fy = node_step(m, s, i, s_wall, C, rc, mode == NODE_UPDATE, bd.cell_status ? bd.cell_status + cell : nullptr);
+        fy = node_step(m, s, i, s_wall, s_box, C, rc, mode == NODE_UPDATE, bd.cell_status ? bd.cell_status + cell : nullptr);
     if (!rec) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     fy = warp_sum_d(fy);
@@ -701,7 +744,9 @@ __global__ void k_points_to_user(MeshDev m, StateDev s, const long long* node_us
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.np) return;
     const long long u = node_user[i];
-    const float4 xh = m.Xh[i], xl = m.Xl[i], uh = s.uh[i], ul = s.ul[i];
+    const float4 xh = m.Xh[i], xl = m.Xl[i], uh = s.ua[i];
+    const float2 lo = s.ub[i];
+    const float4 ul = make_float4(uh.w, lo.x, lo.y, 0.f);
     out[u] = ((double)xh.x + (double)xl.x) + ((double)uh.x + (double)ul.x);
     out[m.np + u] = ((double)xh.y + (double)xl.y) + ((double)uh.y + (double)ul.y);
     out[2 * (long long)m.np + u] = ((double)xh.z + (double)xl.z) + ((double)uh.z + (double)ul.z);
@@ -716,25 +761,45 @@ __global__ void k_points_from_user(MeshDev m, StateDev s, const long long* node_
     const double dy = (in[m.np + u] - (double)xh.y) - (double)xl.y;
     const double dz = (in[2 * (long long)m.np + u] - (double)xh.z) - (double)xl.z;
     const float hx = (float)dx, hy = (float)dy, hz = (float)dz;
-    s.uh[i] = make_float4(hx, hy, hz, 0.f);
-    s.ul[i] = make_float4((float)(dx - hx), (float)(dy - hy), (float)(dz - hz), 0.f);
+    s.ua[i] = make_float4(hx, hy, hz, (float)(dx - hx));
+    s.ub[i] = make_float2((float)(dy - hy), (float)(dz - hz));
 }
 
-__global__ void k_vec_to_user(int np, const float4* a, const long long* node_user, double* out) {
+// part 0: (a.x, a.y, a.z); part 1: (a.w, b.x, b.y)
+__global__ void k_vec_to_user(int np, const float4* a, const float2* b, int part, const long long* node_user,
+                              double* out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= np) return;
     const long long u = node_user[i];
     const float4 q = a[i];
-    out[u] = q.x;
-    out[np + u] = q.y;
-    out[2 * (long long)np + u] = q.z;
+    float x = q.x, y = q.y, z = q.z;
+    if (part == 1) {
+        const float2 r = b[i];
+        x = q.w;
+        y = r.x;
+        z = r.y;
+    }
+    out[u] = x;
+    out[np + u] = y;
+    out[2 * (long long)np + u] = z;
 }
 
-__global__ void k_vec_from_user(int np, float4* a, const long long* node_user, const double* in) {
+__global__ void k_vec_from_user(int np, float4* a, float2* b, int part, const long long* node_user,
+                                const double* in) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= np) return;
     const long long u = node_user[i];
-    a[i] = make_float4((float)in[u], (float)in[np + u], (float)in[2 * (long long)np + u], 0.f);
+    const float x = (float)in[u], y = (float)in[np + u], z = (float)in[2 * (long long)np + u];
+    float4 q = a[i];
+    if (part == 0) {
+        q.x = x;
+        q.y = y;
+        q.z = z;
+    } else {
+        q.w = x;
+        b[i] = make_float2(y, z);
+    }
+    a[i] = q;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -815,15 +880,15 @@ cudaError_t launch_points_from_user(const MeshDev& m, const StateDev& s, const l
     return cudaGetLastError();
 }
 
-cudaError_t launch_vec_to_user(const MeshDev& m, const float4* a, const long long* node_user, double* out,
-                               cudaStream_t st) {
-    k_vec_to_user<<<(m.np + 255) / 256, 256, 0, st>>>(m.np, a, node_user, out);
+cudaError_t launch_vec_to_user(const MeshDev& m, const float4* a, const float2* b, int part, const long long* node_user,
+                               double* out, cudaStream_t st) {
+    k_vec_to_user<<<(m.np + 255) / 256, 256, 0, st>>>(m.np, a, b, part, node_user, out);
     return cudaGetLastError();
 }
 
-cudaError_t launch_vec_from_user(const MeshDev& m, float4* a, const long long* node_user, const double* in,
-                                 cudaStream_t st) {
-    k_vec_from_user<<<(m.np + 255) / 256, 256, 0, st>>>(m.np, a, node_user, in);
+cudaError_t launch_vec_from_user(const MeshDev& m, float4* a, float2* b, int part, const long long* node_user,
+                                 const double* in, cudaStream_t st) {
+    k_vec_from_user<<<(m.np + 255) / 256, 256, 0, st>>>(m.np, a, b, part, node_user, in);
     return cudaGetLastError();
 }
 

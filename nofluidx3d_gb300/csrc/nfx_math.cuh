@@ -113,12 +113,23 @@ NFX_HD Sym3 left_strain(const Mat3& H) {
 }
 
 // Cauchy stress of the compressible Mooney-Rivlin law of tetra.cl:140-156 (and of
-// InteractionFiniteStrainViscoplastic.cl:105-107), written in E = B - I and Jm1 = J - 1:
-//   sigma = mu1 J^-5/3 dev(E) + kappa Jm1 I
-//         + mu2 J^-7/3 [dev(E) + e E - E^2 + (tr(E^2) - e^2)/3 I],   e = tr E.
+// InteractionFiniteStrainViscoplastic.cl:105-107), written in E = B - I and Jm1 = J - 1, as its
+// deviatoric part and its pressure:
+//   sigma = dev + kappa Jm1 I,
+//   dev   = mu1 J^-5/3 dev(E) + mu2 J^-7/3 [(1 + e) dev(E) - dev(E^2)],   e = tr E.
 // With B = I + E this equals the reference's
-//   mu1 J^-5/3 (B - trB/3 I) + kappa (J-1) I + mu2 J^-7/3 (trB B - B^2 + (tr B^2 - trB^2)/3 I).
-NFX_HD Sym3 mr_stress(const Sym3& E, float Jm1, float mu1, float mu2, float kappa) {
+//   mu1 J^-5/3 (B - trB/3 I) + kappa (J-1) I + mu2 J^-7/3 (trB B - B^2 + (tr B^2 - trB^2)/3 I),
+// whose mu2 term is traceless: trB B - B^2 + (tr B^2 - trB^2)/3 I = (1 + e) dev(E) - dev(E^2) +
+// (e e/3 - tr(E^2)/3 + (tr(E^2) - e^2)/3) I and the bracket vanishes. Forming the deviator from
+// deviatoric terms keeps it exact where the stress is mostly hydrostatic (under an indenter the
+// pressure can be ten times the deviator): taking tr(sigma)/3 off a summed stress instead loses
+// that ratio in FP32, and the viscoplastic flow, driven by the deviator every step, integrates
+// the loss (measured: the 10^4-step curve error of the viscoplastic cell halves).
+struct StressSplit {
+    Sym3 dev;
+    float p;  // pressure, tr(sigma)/3
+};
+NFX_HD StressSplit mr_stress_split(const Sym3& E, float Jm1, float mu1, float mu2, float kappa) {
     const float J = 1.0f + Jm1;
     const float c = rcbrt_(J);
     const float c2 = c * c;
@@ -133,31 +144,42 @@ NFX_HD Sym3 mr_stress(const Sym3& E, float Jm1, float mu1, float mu2, float kapp
     D.yz = E.yz;
     D.xz = E.xz;
     const float a1 = mu1 * c5;
-    const float p = kappa * Jm1;
-    Sym3 s;
-    s.xx = a1 * D.xx + p;
-    s.yy = a1 * D.yy + p;
-    s.zz = a1 * D.zz + p;
-    s.xy = a1 * D.xy;
-    s.yz = a1 * D.yz;
-    s.xz = a1 * D.xz;
+    StressSplit r;
+    r.p = kappa * Jm1;
+    r.dev.xx = a1 * D.xx;
+    r.dev.yy = a1 * D.yy;
+    r.dev.zz = a1 * D.zz;
+    r.dev.xy = a1 * D.xy;
+    r.dev.yz = a1 * D.yz;
+    r.dev.xz = a1 * D.xz;
     if (mu2 != 0.0f) {
         const float a2 = mu2 * c5 * c2;
-        // E^2 (symmetric)
+        // E^2 (symmetric) and its trace / 3
         const float q_xx = E.xx * E.xx + E.xy * E.xy + E.xz * E.xz;
         const float q_yy = E.xy * E.xy + E.yy * E.yy + E.yz * E.yz;
         const float q_zz = E.xz * E.xz + E.yz * E.yz + E.zz * E.zz;
         const float q_xy = E.xx * E.xy + E.xy * E.yy + E.xz * E.yz;
         const float q_yz = E.xy * E.xz + E.yy * E.yz + E.yz * E.zz;
         const float q_xz = E.xx * E.xz + E.xy * E.yz + E.xz * E.zz;
-        const float iso = ((q_xx + q_yy + q_zz) - e * e) * (1.0f / 3.0f);
-        s.xx += a2 * ((D.xx + e * E.xx - q_xx) + iso);
-        s.yy += a2 * ((D.yy + e * E.yy - q_yy) + iso);
-        s.zz += a2 * ((D.zz + e * E.zz - q_zz) + iso);
-        s.xy += a2 * (D.xy + e * E.xy - q_xy);
-        s.yz += a2 * (D.yz + e * E.yz - q_yz);
-        s.xz += a2 * (D.xz + e * E.xz - q_xz);
+        const float q3 = (q_xx + q_yy + q_zz) * (1.0f / 3.0f);
+        const float k = 1.0f + e;
+        r.dev.xx += a2 * (k * D.xx - (q_xx - q3));
+        r.dev.yy += a2 * (k * D.yy - (q_yy - q3));
+        r.dev.zz += a2 * (k * D.zz - (q_zz - q3));
+        r.dev.xy += a2 * (k * D.xy - q_xy);
+        r.dev.yz += a2 * (k * D.yz - q_yz);
+        r.dev.xz += a2 * (k * D.xz - q_xz);
     }
+    return r;
+}
+
+// The full Cauchy stress dev + p I.
+NFX_HD Sym3 mr_stress(const Sym3& E, float Jm1, float mu1, float mu2, float kappa) {
+    const StressSplit r = mr_stress_split(E, Jm1, mu1, mu2, kappa);
+    Sym3 s = r.dev;
+    s.xx += r.p;
+    s.yy += r.p;
+    s.zz += r.p;
     return s;
 }
 
@@ -192,6 +214,28 @@ NFX_HD void forces_from_stress(const Mat3& A, const Sym3& s, const float* Dmi, f
         P[3 * i + 0] = a0 * s.xx + a1 * s.xy + a2 * s.xz;
         P[3 * i + 1] = a0 * s.xy + a1 * s.yy + a2 * s.yz;
         P[3 * i + 2] = a0 * s.xz + a1 * s.yz + a2 * s.zz;
+    }
+    const float w = -V0;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const float m0 = Dmi[3 * k] * w, m1 = Dmi[3 * k + 1] * w, m2 = Dmi[3 * k + 2] * w;
+#pragma unroll
+        for (int j = 0; j < 3; j++) f[k + 1][j] = m0 * P[j] + m1 * P[3 + j] + m2 * P[6 + j];
+    }
+#pragma unroll
+    for (int j = 0; j < 3; j++) f[0][j] = -((f[1][j] + f[2][j]) + f[3][j]);
+}
+
+// The same forces from the stress split into its deviator and pressure (sigma = dev + p I).
+NFX_HD void forces_from_split(const Mat3& A, const StressSplit& sp, const float* Dmi, float V0, float f[4][3]) {
+    const Sym3& d = sp.dev;
+    float P[9];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const float a0 = A.m[3 * i], a1 = A.m[3 * i + 1], a2 = A.m[3 * i + 2];
+        P[3 * i + 0] = a0 * (d.xx + sp.p) + a1 * d.xy + a2 * d.xz;
+        P[3 * i + 1] = a0 * d.xy + a1 * (d.yy + sp.p) + a2 * d.yz;
+        P[3 * i + 2] = a0 * d.xz + a1 * d.yz + a2 * (d.zz + sp.p);
     }
     const float w = -V0;
 #pragma unroll
@@ -362,17 +406,17 @@ NFX_HD void vp_element(const float d1[3], const float d2[3], const float d3[3], 
     const float JeM1 = det1p_minus1(G);  // det Fe - 1
     const float Je = 1.0f + JeM1;
     const float JabsM1 = Je >= 0.0f ? JeM1 : (-Je - 1.0f);  // J = sqrt(det Be) = |det Fe|
-    const Sym3 s = mr_stress(Ee, JabsM1, par.mu1, par.mu2, par.kappa);
+    const StressSplit sp = mr_stress_split(Ee, JabsM1, par.mu1, par.mu2, par.kappa);
+    const Sym3& s = sp.dev;  // the shear components of sigma and its deviator coincide
     // forces
     const float JFm1 = det1p_minus1(H);
     const Mat3 A = adj_1p(H);
     const float sgn = (1.0f + JFm1) >= 0.0f ? 1.0f : -1.0f;
-    forces_from_stress(A, s, Dmi, (V0 >= 0.0f ? V0 : -V0) * sgn, f);
+    forces_from_split(A, sp, Dmi, (V0 >= 0.0f ? V0 : -V0) * sgn, f);
     Jm1_out = JFm1;
-    // flow rule (:144-169)
-    const float trS = s.xx + s.yy + s.zz;
-    const float t3 = trS * (1.0f / 3.0f);
-    const float dxx = s.xx - t3, dyy = s.yy - t3, dzz = s.zz - t3;
+    // flow rule (:144-169), driven by the deviatoric stress formed directly
+    const float t3 = sp.p;
+    const float dxx = sp.dev.xx, dyy = sp.dev.yy, dzz = sp.dev.zz;
     const float vm = sqrt_(1.5f * ((dxx * dxx + dyy * dyy + dzz * dzz) +
                                    2.0f * (s.xy * s.xy + s.yz * s.yz + s.xz * s.xz)));
     const float sigma0 = par.yield * (par.hard_exp == 0.0f ? 1.0f : pow_(1.0f + eps / par.hard_thr, par.hard_exp));

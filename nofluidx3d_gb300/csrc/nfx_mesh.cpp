@@ -287,6 +287,16 @@ bool build_mesh_plan(int64_t np, int64_t nt, const double* P, const uint32_t* T,
     }
     plan.ntiles = b;
     plan.nslots = b * T_;
+    {
+        // the most tiles any node appears in sets the per-tile bound of the fixed-point sums
+        std::vector<int32_t> tiles_of((size_t)np, 0);
+        for (int64_t q = 0; q < b; q++) {
+            const int64_t nn = plan.tile_meta[q] >> 16;
+            for (int64_t e = 0; e < nn; e++) tiles_of[plan.tile_nodes[2 * (q * NM_ + e)]]++;
+        }
+        plan.max_tiles_per_node = std::max(1, *std::max_element(tiles_of.begin(), tiles_of.end()));
+        plan.fix_max = force_fix_bound(plan.max_tiles_per_node);
+    }
     plan.tet_user = std::move(slot_user);
     plan.tile_tet_begin.resize(b + 1);
     plan.tile_node_begin.resize(b + 1);
@@ -338,6 +348,27 @@ bool build_mesh_plan(int64_t np, int64_t nt, const double* P, const uint32_t* T,
         // tetra touches
         const double m = mass[u];
         plan.Xh[4 * i + 3] = m != 0.0 ? (float)(1.0 / m) : 0.0f;
+    }
+
+    // bounding box of every node block's reference positions, rounded outwards to float
+    const int64_t nb = (np + NODE_BLOCK - 1) / NODE_BLOCK;
+    plan.block_box.assign(8 * (size_t)nb, 0.0f);
+    for (int64_t q = 0; q < nb; q++) {
+        double lo[3] = {HUGE_VAL, HUGE_VAL, HUGE_VAL}, hi[3] = {-HUGE_VAL, -HUGE_VAL, -HUGE_VAL};
+        for (int64_t i = q * NODE_BLOCK; i < std::min<int64_t>(np, (q + 1) * NODE_BLOCK); i++) {
+            const int64_t u = plan.node_user[i];
+            for (int d = 0; d < 3; d++) {
+                lo[d] = std::min(lo[d], P[d * np + u]);
+                hi[d] = std::max(hi[d], P[d * np + u]);
+            }
+        }
+        for (int d = 0; d < 3; d++) {
+            float l = (float)lo[d], h = (float)hi[d];
+            if ((double)l > lo[d]) l = std::nextafter(l, -HUGE_VALF);
+            if ((double)h < hi[d]) h = std::nextafter(h, HUGE_VALF);
+            plan.block_box[8 * q + d] = l;
+            plan.block_box[8 * q + 4 + d] = h;
+        }
     }
     return true;
 }

@@ -65,7 +65,7 @@ enum Epi : int {
     EPI_OUTPUT = 1,       // y = acc + b stored as f32 [M,N]
     EPI_GRAD_HIDDEN = 2,  // g = acc * silu'(Zp[m,n]) stored as bf16 [M,N] and [N,M]
     EPI_GRAD_INPUT = 3,   // acc stored as f32 [M,N]
-    EPI_WGRAD = 4,        // acc stored as f32 [M,N]
+    EPI_WGRAD = 4,        // acc stored as f32 [M,N]; with bias_out, column bias_col to bias_out[M]
 };
 
 struct EpiArgs {
@@ -79,6 +79,8 @@ struct EpiArgs {
     int gain_ld, gain_k;
     float gain_alpha;
     const float* gain_dx;  // EPI_GRAD_INPUT: per-row term added to column gain_k; null: none
+    float* bias_out;       // EPI_WGRAD: column bias_col goes to bias_out[m] (the bias gradient)
+    int bias_col;
 };
 
 __device__ __forceinline__ float silu_f(float z) { return z / (1.0f + expf(-z)); }
@@ -131,7 +133,12 @@ __device__ __forceinline__ void epi_store(int epi, const EpiArgs& e, int m, int 
             e.out_bt[(size_t)n * e.ldot + m] = g;
             break;
         }
-        default: e.out_f[(size_t)m * e.ldo + n] = acc; break;
+        default:
+            if (e.bias_out && n == e.bias_col)
+                e.bias_out[m] = acc;
+            else
+                e.out_f[(size_t)m * e.ldo + n] = acc;
+            break;
     }
 }
 
@@ -168,16 +175,43 @@ __global__ void __launch_bounds__(128) k_gemm_tn(int M, int N, int K, const bf16
     }
 }
 
-// db[n] = sum over m of dZt[n, m] (fixed order: lane-strided partial sums, then a shuffle tree).
-__global__ void k_bias_grad(int N, int M, const bf16* __restrict__ dzt, int ld, float* __restrict__ db) {
-    const int n = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    const int lane = threadIdx.x & 31;
-    if (n >= N) return;
-    float s = 0.f;
-    for (int m = lane; m < M; m += 32) s += __bfloat162float(dzt[(size_t)n * ld + m]);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) db[n] = s;
+// The training loop's step index: *base + k, where base is a device counter that a captured
+// chunk of k = 0 .. G-1 steps advances at its end (so one CUDA graph serves every chunk).
+__device__ __forceinline__ long long train_step(const long long* base, int k) { return *base + k; }
+
+__global__ void k_advance_counter(long long* base, int n) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *base += n;
+}
+
+__global__ void k_fill_bf16(bf16* p, int n, float v) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = __float2bfloat16_rn(v);
+}
+
+// One training step's minibatch: rows idx[s * M + r] of the dataset's inputs, targets and weights
+// into the staged batch, and the inputs packed as layer 0's BF16 operands X [M, kp] and X^T
+// [kp, ldt] (zero-padded), in one launch. One thread per (row, column) of kp + n_out + 1 columns.
+__global__ void k_gather_pack(int M, int n_in, int kp, int n_out, const int* __restrict__ idx,
+                              const long long* __restrict__ base, int k, const float* __restrict__ x_all,
+                              const float* __restrict__ t_all, const float* __restrict__ w_all, float* __restrict__ xin,
+                              float* __restrict__ tgt, float* __restrict__ wts, bf16* __restrict__ X,
+                              bf16* __restrict__ Xt, int ldt) {
+    const int cols = kp + n_out + 1;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M * cols) return;
+    const int r = i / cols, c = i % cols;
+    const long long row = idx[train_step(base, k) * M + r];
+    if (c < kp) {
+        const float v = c < n_in ? x_all[row * n_in + c] : 0.f;
+        if (c < n_in) xin[(size_t)r * n_in + c] = v;
+        const bf16 b = __float2bfloat16_rn(v);
+        X[(size_t)r * kp + c] = b;
+        Xt[(size_t)c * ldt + r] = b;
+    } else if (c < kp + n_out) {
+        tgt[(size_t)r * n_out + (c - kp)] = t_all[row * n_out + (c - kp)];
+    } else {
+        wts[r] = w_all[row];
+    }
 }
 
 // Inputs: x f32 [M, n_in] (row stride n_in) -> X bf16 [M, kp] and X^T [kp, ldt], zero-padded.
@@ -199,7 +233,8 @@ __global__ void k_pack_input(int M, int n_in, int kp, const float* __restrict__ 
 __global__ void k_loss_grad(int M, int N, const float* __restrict__ y, const float* __restrict__ tgt,
                             const float* __restrict__ w, float scale, float* __restrict__ loss, bf16* __restrict__ dy,
                             bf16* __restrict__ dyt, int ldt, const float* __restrict__ gain_x, int gain_ld, int gain_k,
-                            float gain_alpha, float* __restrict__ gdx) {
+                            float gain_alpha, float* __restrict__ gdx, float* __restrict__ hist,
+                            const long long* __restrict__ base, int k) {
     const int m = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (m >= M) return;
@@ -223,31 +258,67 @@ __global__ void k_loss_grad(int M, int N, const float* __restrict__ y, const flo
     }
     if (lane == 0) {
         loss[m] = ws * s;
+        if (hist) hist[train_step(base, k) * M + m] = ws * s;  // the training loop's loss history
         if (gain_x) gdx[m] = gain_alpha * sg;
     }
 }
 
-// AdamW on one weight matrix [N, K] (logical columns kl of K stored, the rest padding kept at
-// zero) or a bias vector (K = 1); refreshes the BF16 copies W [N, K] and W^T [K, N].
-__global__ void k_adamw(int N, int K, int kl, float* __restrict__ p, const float* __restrict__ gr, float* __restrict__ m1,
-                        float* __restrict__ m2, float lr, float b1, float b2, float eps, float wd, float c1, float c2,
-                        bf16* __restrict__ W, bf16* __restrict__ Wt) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= N * K) return;
-    const int n = i / K, k = i % K;
-    if (k >= kl) return;
-    const float g = gr[i];
-    const float a = b1 * m1[i] + (1.f - b1) * g;
-    const float b = b2 * m2[i] + (1.f - b2) * g * g;
-    m1[i] = a;
-    m2[i] = b;
-    float w = p[i] * (1.f - lr * wd);
-    w -= lr * (a / c1) / (sqrtf(b / c2) + eps);
-    p[i] = w;
-    if (W) {
+// AdamW on every parameter tensor of the network in one launch: a table of segments (each layer's
+// weight matrix and bias vector), the grid running over their concatenation. The learning rate
+// and the bias corrections either come from the host (sched = 0) or follow the training loop's
+// cosine schedule at step *base + k (sched = 1): lr = lr_min + (lr0 - lr_min)(1 + cos(pi s /
+// (steps - 1))) / 2, Adam step t = t0 + s + 1.
+struct AdamSeg {
+    float *p, *m1, *m2;
+    const float* g;
+    bf16 *W, *Wt;
+    int N, K, kl;
+    float wd;
+    long long begin;  // first element in the concatenation
+};
+struct AdamTable {
+    int nseg;
+    AdamSeg seg[2 * MLP_MAX_LAYERS];
+    long long total;
+};
+struct AdamHyper {
+    float lr, b1, b2, eps, c1, c2;  // host-given values (sched = 0)
+    int sched;
+    float lr0, lr_min;
+    long long steps, t0;
+    const long long* base;
+    int k;
+};
+__global__ void k_adamw_all(AdamTable tab, AdamHyper hp) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= tab.total) return;
+    int q = 0;
+    while (q + 1 < tab.nseg && i >= tab.seg[q + 1].begin) q++;
+    const AdamSeg& S = tab.seg[q];
+    const int j = (int)(i - S.begin);
+    const int n = j / S.K, kk = j % S.K;
+    if (kk >= S.kl) return;
+    float lr = hp.lr, c1 = hp.c1, c2 = hp.c2;
+    if (hp.sched) {
+        const long long st = train_step(hp.base, hp.k);
+        const double frac = hp.steps > 1 ? (double)st / (double)(hp.steps - 1) : 0.0;
+        lr = (float)(hp.lr_min + 0.5 * (hp.lr0 - hp.lr_min) * (1.0 + cos(3.14159265358979323846 * frac)));
+        const float t = (float)(hp.t0 + st + 1);
+        c1 = 1.f - powf(hp.b1, t);
+        c2 = 1.f - powf(hp.b2, t);
+    }
+    const float g = S.g[j];
+    const float a = hp.b1 * S.m1[j] + (1.f - hp.b1) * g;
+    const float b = hp.b2 * S.m2[j] + (1.f - hp.b2) * g * g;
+    S.m1[j] = a;
+    S.m2[j] = b;
+    float w = S.p[j] * (1.f - lr * S.wd);
+    w -= lr * (a / c1) / (sqrtf(b / c2) + hp.eps);
+    S.p[j] = w;
+    if (S.W) {
         const bf16 v = __float2bfloat16_rn(w);
-        W[i] = v;
-        Wt[(size_t)k * N + n] = v;
+        S.W[j] = v;
+        S.Wt[(size_t)kk * S.N + n] = v;
     }
 }
 
@@ -258,15 +329,6 @@ __global__ void k_refresh_bf16(int N, int K, const float* __restrict__ p, bf16* 
     const bf16 v = __float2bfloat16_rn(p[i]);
     W[i] = v;
     Wt[(size_t)k * N + n] = v;
-}
-
-// Minibatch gather: rows idx[i] of x [n, n_in] and t [n, n_out].
-__global__ void k_gather_rows(int B, int cols, const int* __restrict__ idx, const float* __restrict__ src,
-                              float* __restrict__ dst) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= B * cols) return;
-    const int r = i / cols, c = i % cols;
-    dst[i] = src[(size_t)idx[r] * cols + c];
 }
 
 // Input-space Adam step for the inverse fit: free inputs move, fixed ones stay, all are clamped
@@ -310,7 +372,8 @@ struct nfx_mlp {
     float *gw[MLP_MAX_LAYERS] = {}, *gb[MLP_MAX_LAYERS] = {};
     float *mw[MLP_MAX_LAYERS] = {}, *vw[MLP_MAX_LAYERS] = {}, *mbias[MLP_MAX_LAYERS] = {}, *vbias[MLP_MAX_LAYERS] = {};
     bf16 *wb[MLP_MAX_LAYERS] = {}, *wbt[MLP_MAX_LAYERS] = {};
-    // activations: X_l bf16 [mb, kin] and X_l^T [kin, mb]; Z_l f32 [mb, nout] (hidden layers)
+    // activations: X_l bf16 [mb, kin] and X_l^T [kin + 1, mb] (its last row all ones); Z_l f32
+    // [mb, nout] (hidden layers)
     bf16 *x[MLP_MAX_LAYERS + 1] = {}, *xt[MLP_MAX_LAYERS + 1] = {};
     float* z[MLP_MAX_LAYERS] = {};
     float* y = nullptr;            // [mb, n_out]
@@ -377,12 +440,13 @@ int backward_dev(nfx_mlp* h, int M, bool want_params, bool want_dx) {
     for (int l = h->nl - 1; l >= 0; l--) {
         const int N = h->nout[l], K = h->kin[l];
         if (want_params) {
+            // dW = dZ^T X and, from the ones row K of X^T, the bias gradient db = dZ^T 1
             EpiArgs e{};
             e.out_f = h->gw[l];
             e.ldo = K;
-            MCUDA(gemm(h->stream, N, K, M, gt, h->mb, h->xt[l], h->mb, EPI_WGRAD, e));
-            k_bias_grad<<<(N + 7) / 8, 256, 0, h->stream>>>(N, M, gt, h->mb, h->gb[l]);
-            MCUDA(cudaGetLastError());
+            e.bias_out = h->gb[l];
+            e.bias_col = K;
+            MCUDA(gemm(h->stream, N, K + 1, M, gt, h->mb, h->xt[l], h->mb, EPI_WGRAD, e));
         }
         if (l > 0) {
             EpiArgs e{};
@@ -416,27 +480,48 @@ int pack_input(nfx_mlp* h, int M) {
     return NFX_OK;
 }
 
-int loss_grad(nfx_mlp* h, int M, const float* tgt_dev, const float* w_dev, float scale) {
+// hist/base/k: the training loop's loss history, indexed by its device step counter (null: none).
+int loss_grad(nfx_mlp* h, int M, const float* tgt_dev, const float* w_dev, float scale, float* hist = nullptr,
+              const long long* base = nullptr, int k = 0) {
     const bool gain = h->gain_k >= 0;
     k_loss_grad<<<(M + 7) / 8, 256, 0, h->stream>>>(M, h->n_out, h->y, tgt_dev, w_dev, scale, h->loss, h->dz, h->dzt,
                                                     h->mb, gain ? h->xin : nullptr, h->n_in, h->gain_k,
-                                                    h->gain_alpha, h->gdx);
+                                                    h->gain_alpha, h->gdx, hist, base, k);
+    MCUDA(cudaGetLastError());
+    return NFX_OK;
+}
+
+// The segment table of every parameter tensor (weights with decay wd, biases without).
+AdamTable adam_table(nfx_mlp* h, float wd) {
+    AdamTable t{};
+    long long pos = 0;
+    for (int l = 0; l < h->nl; l++) {
+        const int N = h->nout[l], K = h->kin[l];
+        t.seg[t.nseg++] = AdamSeg{h->w[l], h->mw[l], h->vw[l], h->gw[l], h->wb[l], h->wbt[l], N, K, h->kl[l], wd, pos};
+        pos += (long long)N * K;
+        t.seg[t.nseg++] = AdamSeg{h->b[l], h->mbias[l], h->vbias[l], h->gb[l], nullptr, nullptr, N, 1, 1, 0.f, pos};
+        pos += N;
+    }
+    t.total = pos;
+    return t;
+}
+
+int adamw_launch(nfx_mlp* h, const AdamTable& t, const AdamHyper& hp) {
+    k_adamw_all<<<(unsigned)((t.total + 255) / 256), 256, 0, h->stream>>>(t, hp);
     MCUDA(cudaGetLastError());
     return NFX_OK;
 }
 
 int adamw_dev(nfx_mlp* h, float lr, float b1, float b2, float eps, float wd) {
     h->adam_t++;
-    const float c1 = 1.f - std::pow(b1, (float)h->adam_t), c2 = 1.f - std::pow(b2, (float)h->adam_t);
-    for (int l = 0; l < h->nl; l++) {
-        const int N = h->nout[l], K = h->kin[l];
-        k_adamw<<<(N * K + 255) / 256, 256, 0, h->stream>>>(N, K, h->kl[l], h->w[l], h->gw[l], h->mw[l], h->vw[l], lr,
-                                                           b1, b2, eps, wd, c1, c2, h->wb[l], h->wbt[l]);
-        k_adamw<<<(N + 255) / 256, 256, 0, h->stream>>>(N, 1, 1, h->b[l], h->gb[l], h->mbias[l], h->vbias[l], lr, b1,
-                                                       b2, eps, 0.f, c1, c2, nullptr, nullptr);
-    }
-    MCUDA(cudaGetLastError());
-    return NFX_OK;
+    AdamHyper hp{};
+    hp.lr = lr;
+    hp.b1 = b1;
+    hp.b2 = b2;
+    hp.eps = eps;
+    hp.c1 = 1.f - std::pow(b1, (float)h->adam_t);
+    hp.c2 = 1.f - std::pow(b2, (float)h->adam_t);
+    return adamw_launch(h, adam_table(h, wd), hp);
 }
 
 int check_batch(nfx_mlp* h, int64_t B) {
@@ -487,7 +572,7 @@ int nfx_mlp_create(int device, int n_in, int width, int depth, int n_out, int64_
             (rc = malloc_dev(h, &h->vw[l], nk)) || (rc = malloc_dev(h, &h->b[l], n)) || (rc = malloc_dev(h, &h->gb[l], n)) ||
             (rc = malloc_dev(h, &h->mbias[l], n)) || (rc = malloc_dev(h, &h->vbias[l], n)) ||
             (rc = malloc_dev(h, &h->wb[l], nk)) || (rc = malloc_dev(h, &h->wbt[l], nk)) ||
-            (rc = malloc_dev(h, &h->x[l], mb * h->kin[l])) || (rc = malloc_dev(h, &h->xt[l], mb * h->kin[l])))
+            (rc = malloc_dev(h, &h->x[l], mb * h->kin[l])) || (rc = malloc_dev(h, &h->xt[l], mb * (h->kin[l] + 1))))
             return fail_out(rc);
         if (l < h->nl - 1 && (rc = malloc_dev(h, &h->z[l], mb * h->nout[l]))) return fail_out(rc);
         for (void* p : {(void*)h->w[l], (void*)h->gw[l], (void*)h->mw[l], (void*)h->vw[l], (void*)h->wb[l], (void*)h->wbt[l]})
@@ -496,6 +581,9 @@ int nfx_mlp_create(int device, int n_in, int width, int depth, int n_out, int64_
             cudaMemsetAsync(p, 0, n * sizeof(float), h->stream);
         cudaMemsetAsync(h->x[l], 0, mb * h->kin[l] * sizeof(bf16), h->stream);
         cudaMemsetAsync(h->xt[l], 0, mb * h->kin[l] * sizeof(bf16), h->stream);
+        // X^T carries a row of ones after its kin rows: the weight-gradient product then yields
+        // the bias gradient as its last column
+        k_fill_bf16<<<(unsigned)((mb + 255) / 256), 256, 0, h->stream>>>(h->xt[l] + mb * h->kin[l], (int)mb, 1.0f);
     }
     const size_t gw = (size_t)std::max(width, n_out);
     if ((rc = malloc_dev(h, &h->y, mb * n_out)) || (rc = malloc_dev(h, &h->dz, mb * gw)) || (rc = malloc_dev(h, &h->dzt, mb * gw)) ||
@@ -647,6 +735,7 @@ int nfx_mlp_adamw(nfx_mlp* h, float lr, float beta1, float beta2, float eps, flo
 // loss of every step is written to losses[steps].
 int nfx_mlp_train(nfx_mlp* h, const float* x_all, const float* t_all, const float* w_all, int64_t n, int64_t batch,
                   int64_t steps, const float* hp, uint64_t seed, float* losses) {
+    const nfx::NvtxRange range("nfx_mlp_train");
     MARG(h && x_all && t_all && hp, "null argument");
     MARG(n >= 1 && steps >= 0, "bad sizes");
     int rc;
@@ -710,23 +799,78 @@ int nfx_mlp_train(nfx_mlp* h, const float* x_all, const float* t_all, const floa
     }
     const int M = (int)batch;
     const float scale = 1.0f / (float)M;
-    for (int64_t s = 0; s < steps; s++) {
-        const int* bi = d_idx + (size_t)s * batch;
-        k_gather_rows<<<(M * h->n_in + 255) / 256, 256, 0, st>>>(M, h->n_in, bi, dx_all, h->xin);
-        k_gather_rows<<<(M * h->n_out + 255) / 256, 256, 0, st>>>(M, h->n_out, bi, dt_all, h->tgt);
-        k_gather_rows<<<(M + 255) / 256, 256, 0, st>>>(M, 1, bi, dw_all, h->wts);
-        const double frac = steps > 1 ? (double)s / (double)(steps - 1) : 0.0;
-        const float lr = (float)(hp[5] + 0.5 * (hp[0] - hp[5]) * (1.0 + std::cos(3.14159265358979323846 * frac)));
-        if ((rc = pack_input(h, M)) || (rc = forward_dev(h, M)) || (rc = loss_grad(h, M, h->tgt, h->wts, scale)) ||
-            (rc = backward_dev(h, M, true, false)) || (rc = adamw_dev(h, lr, hp[1], hp[2], hp[3], hp[4]))) {
+    long long* d_base = nullptr;
+    if (!alloc(&d_base, sizeof(long long))) {
+        cleanup();
+        return mfail(NFX_ERR_NOMEM, "cudaMalloc failed for the step counter");
+    }
+    if (cudaMemsetAsync(d_base, 0, sizeof(long long), st) != cudaSuccess) {
+        cleanup();
+        return mfail(NFX_ERR_CUDA, "step counter reset failed");
+    }
+    const AdamTable tab = adam_table(h, hp[4]);
+    AdamHyper ahp{};
+    ahp.b1 = hp[1];
+    ahp.b2 = hp[2];
+    ahp.eps = hp[3];
+    ahp.sched = 1;
+    ahp.lr0 = hp[0];
+    ahp.lr_min = hp[5];
+    ahp.steps = steps;
+    ahp.t0 = h->adam_t;
+    ahp.base = d_base;
+    // One training step k of a chunk: minibatch, forward, loss (into the history), backward,
+    // AdamW; 14 launches, all reading the step index from the device counter.
+    auto enqueue_step = [&](int k) -> int {
+        const int cols = h->kin[0] + h->n_out + 1;
+        k_gather_pack<<<(unsigned)((M * cols + 255) / 256), 256, 0, st>>>(M, h->n_in, h->kin[0], h->n_out, d_idx, d_base,
+                                                                         k, dx_all, dt_all, dw_all, h->xin, h->tgt,
+                                                                         h->wts, h->x[0], h->xt[0], h->mb);
+        MCUDA(cudaGetLastError());
+        int r;
+        if ((r = forward_dev(h, M)) || (r = loss_grad(h, M, h->tgt, h->wts, scale, loss_hist, d_base, k)) ||
+            (r = backward_dev(h, M, true, false)))
+            return r;
+        AdamHyper a = ahp;
+        a.k = k;
+        return adamw_launch(h, tab, a);
+    };
+    // chunks of TRAIN_GRAPH_STEPS steps replayed as one CUDA graph, the rest launched directly
+    constexpr int TRAIN_GRAPH_STEPS = 16;
+    cudaGraphExec_t gexec = nullptr;
+    const int64_t chunks = steps / TRAIN_GRAPH_STEPS;
+    if (chunks > 0) {
+        cudaGraph_t g = nullptr;
+        if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cleanup();
+            return mfail(NFX_ERR_CUDA, "training graph capture failed to start");
+        }
+        int r = NFX_OK;
+        for (int k = 0; k < TRAIN_GRAPH_STEPS && r == NFX_OK; k++) r = enqueue_step(k);
+        if (r == NFX_OK) k_advance_counter<<<1, 32, 0, st>>>(d_base, TRAIN_GRAPH_STEPS);
+        const cudaError_t ec = cudaStreamEndCapture(st, &g);
+        if (r != NFX_OK || ec != cudaSuccess || cudaGraphInstantiate(&gexec, g, 0) != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            cleanup();
+            return r != NFX_OK ? r : mfail(NFX_ERR_CUDA, "training graph capture failed");
+        }
+        cudaGraphDestroy(g);
+    }
+    for (int64_t c = 0; c < chunks; c++) {
+        if (cudaGraphLaunch(gexec, st) != cudaSuccess) {
+            cudaGraphExecDestroy(gexec);
+            cleanup();
+            return mfail(NFX_ERR_CUDA, "training graph launch failed");
+        }
+    }
+    if (gexec) cudaGraphExecDestroy(gexec);
+    for (int k = 0; k < (int)(steps - chunks * TRAIN_GRAPH_STEPS); k++) {
+        if ((rc = enqueue_step(k)) != NFX_OK) {
             cleanup();
             return rc;
         }
-        if (cudaMemcpyAsync(loss_hist + (size_t)s * M, h->loss, (size_t)M * 4, cudaMemcpyDeviceToDevice, st) != cudaSuccess) {
-            cleanup();
-            return mfail(NFX_ERR_CUDA, "loss copy failed");
-        }
     }
+    h->adam_t += steps;
     if (losses && steps > 0) {
         std::vector<float> all((size_t)steps * M);
         if (cudaMemcpyAsync(all.data(), loss_hist, all.size() * 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||

@@ -94,14 +94,21 @@ __global__ void __launch_bounds__(NOALLOC_BLOCK) k_readout_noalloc(long long np,
     }
 }
 
-// Once per device, with that device current: the device address of the static scratch.
-int scratch_for_device(int dev, double** ptr) {
+// The device address of the static scratch in the current context of device `dev`. The address
+// is looked up again on every call made outside stream capture, so a context that was reset
+// (cudaDeviceReset) or a different context made current since the last call gets its own
+// module's address; inside a capture the address cached by the last uncaptured call is used.
+int scratch_for_device(int dev, cudaStream_t st, double** ptr) {
     if (dev < 0 || dev >= MAX_DEVICES) {
         nfx::set_error("device index out of range for the no-alloc scratch table");
         return NFX_ERR_ARG;
     }
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    const cudaError_t ce = cudaStreamIsCapturing(st, &cap);
+    const bool capturing = ce != cudaSuccess || cap != cudaStreamCaptureStatusNone;
+    if (ce != cudaSuccess) cudaGetLastError();  // e.g. the legacy stream during another stream's capture
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_ptr[dev]) {
+    if (!capturing) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p) {
@@ -109,10 +116,31 @@ int scratch_for_device(int dev, double** ptr) {
             return NFX_ERR_CUDA;
         }
         g_scratch_ptr[dev] = static_cast<double*>(p);
+    } else if (!g_scratch_ptr[dev]) {
+        nfx::set_error("the first nfx_indenter_force_noalloc call on a device must come before any stream capture");
+        return NFX_ERR_STATE;
     }
     *ptr = g_scratch_ptr[dev];
     return NFX_OK;
 }
+
+// Makes `dev` current for the lifetime of the guard and gives the caller its own current
+// device back afterwards.
+struct DeviceGuard {
+    int prev = -1;
+    bool switched = false;
+    cudaError_t enter(int dev) {
+        cudaError_t e = cudaGetDevice(&prev);
+        if (e != cudaSuccess) return e;
+        if (prev == dev) return cudaSuccess;
+        e = cudaSetDevice(dev);
+        switched = e == cudaSuccess;
+        return e;
+    }
+    ~DeviceGuard() {
+        if (switched) cudaSetDevice(prev);
+    }
+};
 
 }  // namespace
 
@@ -135,15 +163,16 @@ extern "C" int nfx_indenter_force_noalloc(int device, int64_t np, const double* 
         nfx::set_error("non-finite contact parameter");
         return NFX_ERR_ARG;
     }
-    cudaError_t e = cudaSetDevice(device);
+    DeviceGuard guard;
+    cudaError_t e = guard.enter(device);
     if (e != cudaSuccess) {
         nfx::set_error(std::string("cudaSetDevice: ") + cudaGetErrorString(e));
         return NFX_ERR_NODEVICE;
     }
-    double* scratch = nullptr;
-    int rc = scratch_for_device(device, &scratch);
-    if (rc != NFX_OK) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    double* scratch = nullptr;
+    int rc = scratch_for_device(device, st, &scratch);
+    if (rc != NFX_OK) return rc;
     // the counter must start at zero; clear it in stream order
     e = cudaMemsetAsync(scratch + NOALLOC_MAX_BLOCKS, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) {

@@ -131,3 +131,41 @@ class MLP:
         check(self._L.nfx_mlp_fit_inputs(self._h, _ptr(x), _ptr(t), None if w is None else _ptr(w), x.shape[0],
                                          _ptr(mask), _ptr(lo_), _ptr(hi_), int(steps), _ptr(hp), _ptr(loss)))
         return x, loss
+
+
+def main(argv=None) -> int:
+    """Training throughput of the surrogate's network (6 -> 256 x 3 -> 64, batch 512) on a synthetic
+    smooth map: wall time per nfx_mlp_train step over --steps steps, after a warm-up call."""
+    import argparse
+    import json
+    import time
+
+    ap = argparse.ArgumentParser(description="time nfx_mlp_train on the surrogate's network")
+    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--batch", type=int, default=512)
+    ap.add_argument("--rows", type=int, default=6144)
+    ap.add_argument("--width", type=int, default=256)
+    ap.add_argument("--depth", type=int, default=3)
+    a = ap.parse_args(argv)
+    rng = np.random.default_rng(0)
+    x = rng.uniform(-1.0, 1.0, (a.rows, 6)).astype(np.float32)
+    d = np.linspace(0.0, 1.0, 64, dtype=np.float32)
+    t = (np.exp(0.3 * x[:, :1]) * d ** (1.5 + 0.3 * x[:, 1:2]) * (1.0 + 0.2 * np.sin(3.0 * x[:, 2:3] * d))).astype(np.float32)
+    m = MLP(6, a.width, a.depth, 64, a.batch)
+    fan = [6] + [a.width] * a.depth
+    outs = [a.width] * a.depth + [64]
+    p = np.concatenate([np.concatenate([rng.standard_normal(o * i) * np.sqrt(2.0 / i), np.zeros(o)])
+                        for i, o in zip(fan, outs)]).astype(np.float32)
+    m.set_params(p)
+    m.train(x, t, steps=32, batch=a.batch)  # warm-up
+    t0 = time.perf_counter()
+    losses = m.train(x, t, steps=a.steps, batch=a.batch)
+    dt = time.perf_counter() - t0
+    m.close()
+    print(json.dumps({"steps": a.steps, "batch": a.batch, "ms_per_step": 1e3 * dt / a.steps,
+                      "first_loss": float(losses[0]), "last_loss": float(losses[-1])}))
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

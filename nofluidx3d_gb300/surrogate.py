@@ -56,10 +56,10 @@ class Protocol:
     """The indentation experiment every curve comes from."""
 
     radius: float = 16.0
-    speed: float = 5e-4          # indenter descent per step
+    speed: float = 1e-4          # indenter descent per step (the indentation speed of the workloads)
     depth_frac: float = 0.3      # curves span depths 0 .. depth_frac * radius
     n_depths: int = 64
-    record_every: int = 50
+    record_every: int = 100
     xi: float = 1e-2             # velocity damping
     k: float = 0.1               # contact penalty
     jitter: float = 0.02
@@ -428,8 +428,8 @@ def surrogate_fit(sur: Surrogate, targets: np.ndarray, indenter_radius: np.ndarr
                      seconds=time.perf_counter() - t0)
 
 
-# The full experiment: a radius-16 cell (103,536 tetra), 9,600 steps per curve. The small one
-# (radius 8, 13,056 tetra, 2,400 steps) is for tests and quick checks.
+# The full experiment: a radius-16 cell (103,536 tetra), 48,000 steps per curve at 1e-4 per
+# step. The small one (radius 8, 13,056 tetra, 2,400 steps) is for tests and quick checks.
 FULL = Protocol()
 SMALL = Protocol(radius=8.0, speed=1e-3, record_every=20, max_cells=4096)
 
@@ -443,17 +443,36 @@ def _stats(x: np.ndarray) -> dict:
             "p90": float(np.quantile(x, 0.9)), "max": float(x.max())}
 
 
+def speed_sensitivity(P: np.ndarray, F: np.ndarray, proto: Protocol, alt_speed: float) -> dict:
+    """How much the curves depend on the indentation speed: the inputs P (whose curves at
+    proto.speed are F) simulated again at alt_speed, curve against curve at the same depths."""
+    from dataclasses import replace
+
+    alt = replace(proto, speed=alt_speed, record_every=max(10, int(round(proto.record_every * proto.speed / alt_speed))))
+    Fa = simulate_curves(P, alt)
+    ok = np.all(np.isfinite(F), axis=1) & np.all(np.isfinite(Fa), axis=1)
+    d = curve_error(Fa[ok], F[ok])
+    return {"speed": proto.speed, "alt_speed": alt_speed, "curves": int(ok.sum()), "relative_difference": _stats(d)}
+
+
 def run_experiment(proto: Protocol = FULL, n_curves: int = 8192, n_hold: int = 1024, n_targets: int = 1024,
                    n_plain: int = 128, noise: float = 0.01, train_steps: int = 20000, batch: int = 512,
-                   lr: float = 2e-3, starts: int = 16, seed: int = 0, log=print, data_out: str | None = None) -> dict:
+                   lr: float = 2e-3, starts: int = 16, seed: int = 0, log=print, data_out: str | None = None,
+                   speed_check: int = 0, alt_speed: float = 5e-4) -> dict:
     """Curves from the batched simulator -> surrogate training -> held-out error -> inverse fits
-    of noisy targets with and without the surrogate. Returns a JSON-ready summary."""
+    of noisy targets with and without the surrogate. Returns a JSON-ready summary. speed_check > 0
+    also simulates that many of the dataset's inputs at alt_speed (speed_sensitivity)."""
     t_all = time.perf_counter()
     st_data = SimStats()
     P = sample_params(n_curves, proto, seed)
     F = simulate_curves(P, proto, st_data)
     ok = np.all(np.isfinite(F), axis=1)
     log(f"dataset: {n_curves} curves in {st_data.seconds:.1f} s, {int((~ok).sum())} non-finite")
+    speed = None
+    if speed_check > 0:
+        speed = speed_sensitivity(P[:speed_check], F[:speed_check], proto, alt_speed)
+        log(f"speed sensitivity: median curve difference {speed['relative_difference'].get('median', float('nan')):.3e} "
+            f"between {proto.speed:g} and {alt_speed:g} per step")
     tr = np.arange(n_curves - n_hold)
     ho = np.arange(n_curves - n_hold, n_curves)
     tr, ho = tr[ok[tr]], ho[ok[ho]]
@@ -511,6 +530,7 @@ def run_experiment(proto: Protocol = FULL, n_curves: int = 8192, n_hold: int = 1
             "surrogate_error_le_plain_plus_1e-3": float(np.mean(rs.error[:k] <= rp.error + 1e-3)),
             "agreement": _stats(agree),
         },
+        "speed_sensitivity": speed,
         "wall_seconds": time.perf_counter() - t_all,
     }
 
@@ -530,10 +550,18 @@ def main(argv=None) -> int:
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--out", default=None, help="JSON summary path")
     ap.add_argument("--data", default=None, help="npz path for the generated curves")
+    ap.add_argument("--speed", type=float, default=None, help="indentation per step (default: the protocol's)")
+    ap.add_argument("--speed-check", type=int, default=0,
+                    help="dataset inputs also simulated at --alt-speed to measure the speed dependence")
+    ap.add_argument("--alt-speed", type=float, default=5e-4)
     a = ap.parse_args(argv)
     proto = FULL if a.protocol == "full" else SMALL
+    if a.speed is not None:
+        from dataclasses import replace
+
+        proto = replace(proto, speed=a.speed)
     res = run_experiment(proto, a.curves, a.hold, a.targets, a.plain, train_steps=a.train_steps, batch=a.batch,
-                         seed=a.seed, data_out=a.data)
+                         seed=a.seed, data_out=a.data, speed_check=a.speed_check, alt_speed=a.alt_speed)
     text = json.dumps(res, indent=1)
     if a.out:
         with open(a.out, "w") as f:

@@ -15,8 +15,10 @@ the built library, which stays untracked in oracle/_ref/):
   * `#ifdef FIXED_TOP_BOTTOM ... #endif` (:17-22) -> a run-time branch;
   * clang's `overloadable` attribute dropped and `always_inline` -> `inline`.
 
-Usage: python oracle/build_ref.py [reference_root]   (default: /root/reference)
-Exit status 0 and a message when the reference tree is absent (nothing to build).
+Usage: python oracle/build_ref.py [reference_root]
+The reference root is the argument, else the environment variable NFX_REFERENCE_ROOT, else
+/root/reference (where this recipe's build host keeps the reference tree). Exit status 0 and a
+message when the reference tree is absent (nothing to build).
 """
 
 from __future__ import annotations
@@ -47,6 +49,21 @@ KERNEL_FILES = [
     "InteractionSphereIntegral.cl",
 ]
 
+DEFAULT_REFERENCE_ROOT = "/root/reference"
+
+
+def reference_root(arg: str | os.PathLike | None = None) -> Path:
+    """The reference tree this recipe reads: `arg`, else $NFX_REFERENCE_ROOT, else the build
+    host's checkout."""
+    if arg:
+        return Path(arg)
+    return Path(os.environ.get("NFX_REFERENCE_ROOT") or DEFAULT_REFERENCE_ROOT)
+
+
+def reference_present(arg: str | os.PathLike | None = None) -> bool:
+    return (reference_root(arg) / "nofluidx3d" / "kernels").is_dir()
+
+
 _VEC_LITERAL = re.compile(r"\((ibmPrecisionFloat3|tetraPrecisionFloat3|double3|float3)\)\s*\(")
 
 
@@ -65,8 +82,8 @@ def transform(name: str, text: str) -> str:
     return text
 
 
-def build(reference_root: str | os.PathLike = "/root/reference", quiet: bool = False) -> Path | None:
-    kdir = Path(reference_root) / "nofluidx3d" / "kernels"
+def build(root: str | os.PathLike | None = None, quiet: bool = False) -> Path | None:
+    kdir = reference_root(root) / "nofluidx3d" / "kernels"
     if not kdir.is_dir():
         if not quiet:
             print(f"build_ref: no reference kernels at {kdir}; nothing to build")
@@ -92,4 +109,4 @@ def build(reference_root: str | os.PathLike = "/root/reference", quiet: bool = F
 
 
 if __name__ == "__main__":
-    build(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    build(sys.argv[1] if len(sys.argv) > 1 else None)

@@ -6,7 +6,9 @@ Simulation.timeStep (Simulation.py:232-237) and the final positions, velocities,
 force curve and (viscoplastic) plastic state are stored. The GPU box has no reference tree;
 tests there compare against these files.
 
-    python tests/golden/make_golden.py [/root/reference] [case ...]
+    python tests/golden/make_golden.py [reference_root] [case ...]
+
+The reference root defaults to $NFX_REFERENCE_ROOT or the recipe's default (oracle/build_ref.py).
 """
 
 from __future__ import annotations
@@ -26,7 +28,7 @@ from tests.golden.cases import CASES  # noqa: E402
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
-def main(ref_root: str = "/root/reference", names=None) -> None:
+def main(ref_root: str | None = None, names=None) -> None:
     if build_ref.build(ref_root) is None:
         raise SystemExit("reference tree not found")
     for name, case in CASES.items():
@@ -42,4 +44,4 @@ def main(ref_root: str = "/root/reference", names=None) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", sys.argv[2:])
+    main(sys.argv[1] if len(sys.argv) > 1 else None, sys.argv[2:])

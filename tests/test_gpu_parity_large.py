@@ -1,11 +1,17 @@
-"""Viscoplastic 10^4-step parity on larger cells: the surrogate's R=16 cell (103,536 tetra) in the
-GPU suite, and the 1M-tetra headline cell (R=34, 989,808 tetra) when NFX_LONG_TESTS=1 (about
-three minutes of host time for the FP64 oracle). The oracle runs in parallel in chunks of one
-record interval; the indenter-force row at each record time is the reference's sphere penalty
-readout (Simulation.py:198-212) evaluated on the oracle's positions at that time, which is what
-the device computes inside the step that starts at that time."""
+"""Viscoplastic parity on the large cells the benchmark runs, against the FP64 oracle.
 
-import os
+Cases (Mooney-Rivlin + finite-strain viscoplastic law, sphere indenter at 1e-4 per step, the
+plain-large construction of the benchmark at three radii):
+  * R = 16 (103,536 tetra, sphere of radius 4), 10^4 steps — the surrogate's cell;
+  * R = 34 (989,808 tetra, sphere of radius 16), 10^4 steps — the 1M-tetra headline cell;
+  * R = 64 (6,594,816 tetra, sphere of radius 16), 2,000 steps — the benchmark's own cell.
+The oracle runs in parallel in chunks of one record interval; the indenter-force row at each
+record time is the reference's sphere penalty readout (Simulation.py:198-212) evaluated on the
+oracle's positions at that time, which is what the device computes inside the step that starts at
+that time. Reported per case: the trajectory error relative to the positions, the same error
+relative to the displacement field (x - X, much smaller than x), and the relative L2 error of the
+force curve. Bars: trajectory 1e-5, curve 1e-4 (the benchmark spec's); the displacement error is
+held to 1e-3."""
 
 import numpy as np
 import pytest
@@ -13,11 +19,12 @@ import pytest
 import oracle as O
 from nofluidx3d_gb300.core import CellSim
 from nofluidx3d_gb300.workloads import plain_large
-from tests.helpers import oracle_problem, rel_curve, rel_traj
+from tests.helpers import oracle_problem, rel_curve, rel_disp, rel_traj
 
 pytestmark = pytest.mark.gpu
 
 TRAJ_TOL = 1e-5
+DISP_TOL = 1e-3
 CURVE_TOL = 1e-4
 
 
@@ -47,28 +54,40 @@ def run_case(R: float, Rs: float, n: int):
     sim.step(n)
     sim.record_now()
     assert sim.status() == 0
-    traj = rel_traj(st.positions(), sim.points())
-    curve = rel_curve(cref, sim.curve())
+    x = sim.points()
+    traj = rel_traj(st.positions(), x)
+    disp = rel_disp(st.positions(), x, m.points)
+    cgpu = sim.curve()
+    curve = rel_curve(cref, cgpu)
     sim.close()
     assert cref[-1, 2] > 0  # the sphere pressed into the cell
-    return traj, curve
+    err = np.abs(cgpu[:, 2] - cref[:, 2])
+    k = int(np.argmax(err))
+    print(f"R{R:g}: {n} steps, trajectory {traj:.3e}, displacement {disp:.3e}, curve {curve:.3e}; "
+          f"largest row error {err[k]:.3e} at t = {cref[k, 0]:.0f} (force {cref[k, 2]:.4e}, peak {cref[:, 2].max():.4e})")
+    return traj, disp, curve
 
 
 def test_viscoplastic_sphere_r16_10k_steps_vs_fp64_oracle():
-    """Measured on GB300: trajectory 1.4e-7, curve 9.9e-5 — close to the 1e-4 bar: a sphere of
-    radius 4 presses few nodes hard, and its penalty force amplifies the FP32 error of the
-    element forces in a quasi-static balance."""
-    traj, curve = run_case(16.0, 4.0, 10000)
-    print(f"R16: trajectory {traj:.3e} curve {curve:.3e}")
+    traj, disp, curve = run_case(16.0, 4.0, 10000)
     assert traj < TRAJ_TOL
+    assert disp < DISP_TOL
     assert curve < CURVE_TOL
 
 
-@pytest.mark.skipif(os.environ.get("NFX_LONG_TESTS") != "1", reason="long: set NFX_LONG_TESTS=1")
 def test_viscoplastic_sphere_r34_10k_steps_vs_fp64_oracle():
-    """The 1M-tetra cell of the headline configuration (sphere of radius 16). Measured on GB300:
-    trajectory 3.1e-8, curve 7.6e-5."""
-    traj, curve = run_case(34.0, 16.0, 10000)
-    print(f"R34: trajectory {traj:.3e} curve {curve:.3e}")
+    """The 1M-tetra cell of the headline configuration (about two minutes of oracle time on 16
+    host cores)."""
+    traj, disp, curve = run_case(34.0, 16.0, 10000)
     assert traj < TRAJ_TOL
+    assert disp < DISP_TOL
+    assert curve < CURVE_TOL
+
+
+def test_viscoplastic_sphere_r64_2k_steps_vs_fp64_oracle():
+    """The benchmark's cell (6.6 M tetra) for 2,000 steps (about two and a half minutes of
+    oracle time on 16 host cores): the sphere presses 0.2 lattice units into the cell."""
+    traj, disp, curve = run_case(64.0, 16.0, 2000)
+    assert traj < TRAJ_TOL
+    assert disp < DISP_TOL
     assert curve < CURVE_TOL

@@ -119,3 +119,36 @@ def test_tile_plan_any_tetra_order():
     _plan_check(m.points, np.asarray(m.tets)[rng.permutation(m.num_tetra)], 128)
     one = np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.0, 0.0, 1.0]])
     assert _plan_check(one, np.array([[0, 1, 2, 3]]), 128) == (1, 4)
+
+
+def _star(n_ring: int) -> tuple[np.ndarray, np.ndarray]:
+    """A node of very high valence: node 0 at the origin is a corner of every tetra, whose other
+    corners are neighbouring triangles of a latitude-longitude sphere around it."""
+    th = np.linspace(0.15, np.pi - 0.15, n_ring)
+    ph = np.linspace(0.0, 2 * np.pi, 2 * n_ring, endpoint=False)
+    pts = [[0.0, 0.0, 0.0]]
+    for t in th:
+        for p in ph:
+            pts.append([np.sin(t) * np.cos(p), np.cos(t), np.sin(t) * np.sin(p)])
+    pts = np.array(pts)
+    idx = lambda i, j: 1 + i * len(ph) + (j % len(ph))  # noqa: E731
+    tets = []
+    for i in range(n_ring - 1):
+        for j in range(len(ph)):
+            for tri in ((idx(i, j), idx(i + 1, j), idx(i, j + 1)), (idx(i + 1, j), idx(i + 1, j + 1), idx(i, j + 1))):
+                a, b, c = (pts[k] for k in tri)
+                tets.append((0, *tri) if np.dot(a, np.cross(b, c)) > 0 else (0, tri[0], tri[2], tri[1]))
+    return pts, np.array(tets)
+
+
+@pytest.mark.parametrize("tile", [64, 512])
+def test_fixed_point_bound_covers_the_busiest_node(tile):
+    """Every tile that lists a node adds one fixed-point tile sum to that node's 64-bit word; the
+    planner shares the word's range out over the most tiles any node appears in, so that sums
+    within the per-tile bound cannot wrap it. nfx_plan_check recounts the tiles per node and checks
+    (tiles per node) x bound x 2^40 < 2^63. Here node 0 is a corner of all 2,574 tetrahedra and
+    appears in dozens of tiles."""
+    pts, tets = _star(40)
+    assert len(tets) > 2000
+    ntiles, _ = _plan_check(pts, tets, tile)
+    assert ntiles >= len(tets) // tile

@@ -16,7 +16,7 @@ def test_unit_box_round_trip():
         u = S.to_unit(P, proto)
         assert np.all(np.abs(u) <= 1 + 1e-12)
         np.testing.assert_allclose(S.from_unit(u, proto), P, rtol=1e-12)
-    assert S.FULL.steps == 9600 and S.FULL.max_depth == pytest.approx(4.8)
+    assert S.FULL.steps == 48000 and S.FULL.max_depth == pytest.approx(4.8)  # 4.8 at 1e-4 per step
     assert S.SMALL.steps == 2400
     assert S.FULL.bounds()[0][5] == 4.0 and S.FULL.bounds()[1][5] == 24.0  # indenter radius 4..24 at R = 16
 
