@@ -54,11 +54,12 @@ constexpr int MLP_MAX_WIDTH = 1024;
 
 // ---------------------------------------------------------------------------------------
 // GEMM: C[M,N] = A[M,K] B[N,K]^T, BF16 operands, FP32 accumulation, fused epilogue.
-// A block of 4 warps covers 64 rows x 32 columns; each warp a 16 x 32 strip (four 16x8 MMA
-// tiles). Operands are read as 32-bit pairs straight from global memory (the matrices of this
-// network live in L2); lda/ldb must be even and the pointers 4-byte aligned. Any K works: pairs
-// at or past K read as zero (the weight-gradient products reduce over the batch, whose
-// transposed buffers hold stale columns beyond it).
+// A block of 4 warps covers 64 rows x 64 columns, each warp 32 x 32 (two m16 row groups x four
+// n8 column groups of mma.sync m16n8k16). K advances in chunks of 64 through two shared-memory
+// stages filled by cp.async (16-byte copies, zero-filled past M, N or K), so a chunk's global
+// loads overlap the previous chunk's MMAs. lda/ldb must be multiples of 8 and the operands
+// 16-byte aligned. Any K works: columns at or past K read as zero (the weight-gradient products
+// reduce over the batch, whose transposed buffers hold stale columns beyond it).
 // ---------------------------------------------------------------------------------------
 enum Epi : int {
     EPI_HIDDEN = 0,       // z = acc + b: Z (f32) stored; a = silu(z) stored as bf16 [M,N] and [N,M]
@@ -89,12 +90,37 @@ __device__ __forceinline__ float silu_grad(float z) {
     return s * (1.0f + z * (1.0f - s));
 }
 
-// The pair (k, k+1) of a row; the element at k sits in the low half.
-__device__ __forceinline__ unsigned ld_pair(const bf16* p, bool ok, int k, int K) {
-    if (!ok || k >= K) return 0u;
-    const unsigned w = *reinterpret_cast<const unsigned*>(p);
-    return k + 1 < K ? w : (w & 0xffffu);
+constexpr int GB_M = 64, GB_N = 64, GB_K = 64;
+// Staged rows are padded to 72 elements (144 B): a warp's fragment loads (rows g = 0..7, pairs
+// q = 0..3 at word 36 g + q) then fall on 32 distinct banks.
+constexpr int GB_LD = GB_K + 8;
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, int src_bytes) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(sa), "l"(gmem), "r"(src_bytes) : "memory");
 }
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// Stage rows [r0, r0 + 64) x columns [k0, k0 + GB_K) of a row-major BF16 matrix (rows x K, leading
+// dimension ld) into s[64][GB_LD]: 512 copies of 8 elements, 4 per thread. Copies past the matrix
+// read nothing (source size 0, from the matrix's own aligned base) and fill zeros.
+__device__ __forceinline__ void stage_tile(bf16* s, const bf16* g, int ld, int r0, int rows, int k0, int K) {
+#pragma unroll
+    for (int c = threadIdx.x; c < 64 * (GB_K / 8); c += 128) {
+        const int r = c / (GB_K / 8), kc = (c % (GB_K / 8)) * 8;
+        const int row = r0 + r, k = k0 + kc;
+        int bytes = 0;
+        const bf16* src = g;
+        if (row < rows && k < K) {
+            bytes = min(8, K - k) * 2;
+            src = g + (size_t)row * ld + k;
+        }
+        cp_async16(s + r * GB_LD + kc, src, bytes);
+    }
+}
+
+__device__ __forceinline__ unsigned lds_pair(const bf16* p) { return *reinterpret_cast<const unsigned*>(p); }
 
 __device__ __forceinline__ void mma_bf16(float (&c)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
     asm volatile(
@@ -144,34 +170,61 @@ __device__ __forceinline__ void epi_store(int epi, const EpiArgs& e, int m, int 
 
 __global__ void __launch_bounds__(128) k_gemm_tn(int M, int N, int K, const bf16* __restrict__ A, int lda,
                                                  const bf16* __restrict__ B, int ldb, int epi, EpiArgs e) {
+    __shared__ __align__(16) bf16 sA[2][GB_M * GB_LD];
+    __shared__ __align__(16) bf16 sB[2][GB_N * GB_LD];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int g = lane >> 2, q = lane & 3;
-    const int m0 = blockIdx.x * 64 + warp * 16;
-    const int n0 = blockIdx.y * 32;
-    float c[4][4] = {};
-    const int ra = m0 + g, rb = m0 + g + 8;
-    for (int k0 = 0; k0 < K; k0 += 16) {
-        const int ka = k0 + 2 * q;
-        unsigned a[4];
-        a[0] = ld_pair(A + (size_t)ra * lda + ka, ra < M, ka, K);
-        a[1] = ld_pair(A + (size_t)rb * lda + ka, rb < M, ka, K);
-        a[2] = ld_pair(A + (size_t)ra * lda + ka + 8, ra < M, ka + 8, K);
-        a[3] = ld_pair(A + (size_t)rb * lda + ka + 8, rb < M, ka + 8, K);
-#pragma unroll
-        for (int t = 0; t < 4; t++) {
-            const int nb = n0 + t * 8 + g;
-            const unsigned b0 = ld_pair(B + (size_t)nb * ldb + ka, nb < N, ka, K);
-            const unsigned b1 = ld_pair(B + (size_t)nb * ldb + ka + 8, nb < N, ka + 8, K);
-            mma_bf16(c[t], a, b0, b1);
+    const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+    const int m0 = blockIdx.x * GB_M, n0 = blockIdx.y * GB_N;
+    float c[2][4][4] = {};
+    const int nk = (K + GB_K - 1) / GB_K;
+    stage_tile(sA[0], A, lda, m0, M, 0, K);
+    stage_tile(sB[0], B, ldb, n0, N, 0, K);
+    cp_async_commit();
+    for (int kc = 0; kc < nk; kc++) {
+        const int cur = kc & 1;
+        if (kc + 1 < nk) {
+            stage_tile(sA[cur ^ 1], A, lda, m0, M, (kc + 1) * GB_K, K);
+            stage_tile(sB[cur ^ 1], B, ldb, n0, N, (kc + 1) * GB_K, K);
         }
+        cp_async_commit();
+        cp_async_wait_prev();  // every group but the newest has landed: chunk kc is staged
+        __syncthreads();
+        const bf16* as = sA[cur];
+        const bf16* bs = sB[cur];
+#pragma unroll
+        for (int ks = 0; ks < GB_K; ks += 16) {
+            unsigned af[2][4];
+#pragma unroll
+            for (int i = 0; i < 2; i++) {
+                const bf16* r0 = as + (wm + i * 16 + g) * GB_LD + ks + 2 * q;
+                const bf16* r8 = r0 + 8 * GB_LD;
+                af[i][0] = lds_pair(r0);
+                af[i][1] = lds_pair(r8);
+                af[i][2] = lds_pair(r0 + 8);
+                af[i][3] = lds_pair(r8 + 8);
+            }
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                const bf16* rb = bs + (wn + t * 8 + g) * GB_LD + ks + 2 * q;
+                const unsigned b0 = lds_pair(rb), b1 = lds_pair(rb + 8);
+                mma_bf16(c[0][t], af[0], b0, b1);
+                mma_bf16(c[1][t], af[1], b0, b1);
+            }
+        }
+        __syncthreads();  // the stage is read out before the next iteration refills it
     }
 #pragma unroll
-    for (int t = 0; t < 4; t++) {
-        const int n = n0 + t * 8 + 2 * q;
-        epi_store(epi, e, ra, n, M, N, c[t][0]);
-        epi_store(epi, e, ra, n + 1, M, N, c[t][1]);
-        epi_store(epi, e, rb, n, M, N, c[t][2]);
-        epi_store(epi, e, rb, n + 1, M, N, c[t][3]);
+    for (int i = 0; i < 2; i++) {
+        const int ra = m0 + wm + i * 16 + g, rb = ra + 8;
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            const int n = n0 + wn + t * 8 + 2 * q;
+            epi_store(epi, e, ra, n, M, N, c[i][t][0]);
+            epi_store(epi, e, ra, n + 1, M, N, c[i][t][1]);
+            epi_store(epi, e, rb, n, M, N, c[i][t][2]);
+            epi_store(epi, e, rb, n + 1, M, N, c[i][t][3]);
+        }
     }
 }
 
@@ -401,7 +454,10 @@ int malloc_dev(nfx_mlp* h, T** p, size_t n) {
 
 cudaError_t gemm(cudaStream_t st, int M, int N, int K, const bf16* A, int lda, const bf16* B, int ldb, int epi,
                  const EpiArgs& e) {
-    const dim3 grid((unsigned)((M + 63) / 64), (unsigned)((N + 31) / 32));
+    // the staged loads copy 16-byte pieces of rows
+    if (lda % 8 || ldb % 8 || (reinterpret_cast<uintptr_t>(A) & 15u) || (reinterpret_cast<uintptr_t>(B) & 15u))
+        return cudaErrorMisalignedAddress;
+    const dim3 grid((unsigned)((M + GB_M - 1) / GB_M), (unsigned)((N + GB_N - 1) / GB_N));
     k_gemm_tn<<<grid, 128, 0, st>>>(M, N, K, A, lda, B, ldb, epi, e);
     return cudaGetLastError();
 }

@@ -148,3 +148,33 @@ def test_cell_status_marks_only_the_failing_cell():
     assert st[1] != 0
     assert b.status() == st[1]
     b.close()
+
+
+def test_batch_material_corners_match_oracle():
+    """The corners of the batched population's material box against the FP64 oracle, in one
+    batch: the softest cell (shear modulus 2e-4, bulk/shear 5, yield 5e-5, viscosity 1e-2), whose
+    nodal forces are the smallest the 2^-40 fixed-point accumulator has to resolve, the stiffest
+    stable one and a middle one, each under its sphere for 2,000 steps."""
+    base = batched_cells(1, seed=11, r_range=(5.0, 5.0), steps=2000)[0].with_(speed=2e-4, record_every=100)
+    corners = [dict(C10=1e-4, K=1e-3, yield_stress=5e-5, viscosity=1e-2),      # mu = 2e-4, K/mu = 5
+               dict(C10=2.5e-3, K=2.5e-2, yield_stress=1e-3, viscosity=1e-1),  # mu = 5e-3, K/mu = 5
+               dict(C10=5e-4, K=2e-2, yield_stress=2e-4, viscosity=3e-2)]      # mu = 1e-3, K/mu = 20
+    cells = [base.with_(seed=20 + i, **c) for i, c in enumerate(corners)]
+    meshes = [w.mesh() for w in cells]
+    b = Batch(0, tile_tets=128)
+    for w, m in zip(cells, meshes):
+        w.add_to_batch(b, m)
+    b.set_record(1, 100, 30)
+    b.finalize()
+    b.step(2000)
+    b.record_now()
+    assert np.all(b.cell_status() == 0)
+    for i, (w, m) in enumerate(zip(cells, meshes)):
+        st = O.State(oracle_problem(w, m), "f64")
+        cref = st.run(2000, 100)
+        assert cref[-1, 2] > 0, i  # the sphere presses into the cell
+        traj, curve = rel_traj(st.positions(), b.points(i)), rel_curve(cref, b.curve(i))
+        print(f"corner {i}: trajectory {traj:.3e} curve {curve:.3e} peak force {cref[:, 2].max():.3e}")
+        assert traj < 1e-5, i
+        assert curve < 1e-4, i
+    b.close()
