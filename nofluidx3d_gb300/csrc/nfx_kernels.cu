@@ -475,6 +475,29 @@ struct WallStep {
 #ifndef NFX_NODE_CULL
 #define NFX_NODE_CULL 1  // 0: every node reads its reference position
 #endif
+// Whether a node block lies within EAGER_REACH lattice units of a contact, judged on its reference
+// box alone (a heuristic for when to read reference positions early; the per-node test above
+// decides what is evaluated, so the answer never changes a result).
+constexpr float EAGER_REACH = 4.0f;
+__device__ __forceinline__ bool block_near(const ContactDev* cs, int nc, const WallStep* wall, float4 lo, float4 hi) {
+    bool near = false;
+    for (int c = 0; c < nc; c++) {
+        const ContactDev& k = cs[c];
+        const float wf = wall[c].wf;
+        if (k.kind == CONTACT_SUBSTRATE) {
+            near |= lo.y - EAGER_REACH < wf;
+        } else if (k.kind == CONTACT_PLANE) {
+            near |= hi.y + EAGER_REACH > wf;
+        } else if (k.kind == CONTACT_SPHERE) {
+            const float dx = fmaxf(fmaxf(lo.x, -hi.x), 0.f), dy = fmaxf(fmaxf(lo.y - wf, wf - hi.y), 0.f),
+                        dz = fmaxf(fmaxf(lo.z, -hi.z), 0.f);
+            const float r = wall[c].rf + EAGER_REACH;
+            near |= dx * dx + dy * dy + dz * dz < r * r;
+        }
+    }
+    return near;
+}
+
 __device__ __forceinline__ bool contact_reaches(const ContactDev& c, const WallStep& ws, float4 lo, float4 hi,
                                                 const float4& uh) {
     if (c.kind == CONTACT_SPHERE_INTEGRAL) return false;  // a per-tetra force (element pass)
@@ -557,10 +580,17 @@ __device__ __forceinline__ bool contact_force(const ContactDev& c, const WallSte
 // displacement carried as hi + lo — damped velocity Verlet with unit mass and the FIXED_TOP_BOTTOM
 // pin (VelocityVerlet.cl), or the lumped-mass form (velocityVerlet2.cl) — and the accumulator reset.
 __device__ __forceinline__ double node_step(const MeshDev& m, const StateDev& s, int i, const WallStep* wall,
-                                           const float4* box, const CellDev& C, int rc, bool update, unsigned* cstat) {
+                                           const float4* box, bool near, const CellDev& C, int rc, bool update,
+                                           unsigned* cstat) {
     const ContactDev* cs = C.c;
     const int nc = C.n_contacts;
     const long long np = m.np;
+    // In a block near a contact (or under the lumped-mass integrator, which needs Xh.w) the
+    // reference position is read with the node's first loads; elsewhere only after the per-node
+    // test below says a contact can reach the node.
+    const bool xh_loaded = near || C.integrator == INTEGRATOR_VV2;
+    float4 xh = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (xh_loaded) xh = m.Xh[i];
     float4 f = make_float4(fix_to_float(s.facc[i]), fix_to_float(s.facc[np + i]), fix_to_float(s.facc[2 * np + i]), 0.f);
     const float4 a = s.ua[i];
     const float2 lo = s.ub[i];
@@ -571,8 +601,7 @@ __device__ __forceinline__ double node_step(const MeshDev& m, const StateDev& s,
     const float4 blo = box[0], bhi = box[1];
     for (int c = 0; c < nc; c++)
         if (contact_reaches(cs[c], wall[c], blo, bhi, uh)) reach |= 1u << c;
-    float4 xh = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (reach || C.integrator == INTEGRATOR_VV2) xh = m.Xh[i];
+    if (!xh_loaded && reach) xh = m.Xh[i];
     double fy_rc = 0.0;
     for (int c = 0; c < nc; c++) {
         double fy;
@@ -670,8 +699,10 @@ __global__ void __launch_bounds__(NODE_BLOCK, NFX_NODE_MIN_BLOCKS) k_node_pass(M
         }
     }
     double fy = 0.0;  // y force of the readout contact on this node
+    const bool near = !NFX_NODE_CULL || block_near(C.c, C.n_contacts, s_wall, s_box[0], s_box[1]);
     if (i < C.node_end)
-        fy = node_step(m, s, i, s_wall, s_box, C, rc, mode == NODE_UPDATE, bd.cell_status ? bd.cell_status + cell : nullptr);
+        fy = node_step(m, s, i, s_wall, s_box, near, C, rc, mode == NODE_UPDATE,
+                       bd.cell_status ? bd.cell_status + cell : nullptr);
     if (!rec) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     fy = warp_sum_d(fy);
