@@ -184,6 +184,54 @@ __device__ __forceinline__ bool node_flush(uint2 node, const unsigned short* inc
     return true;
 }
 
+// The flush with each tile node's incidence run split over two adjacent lanes: lane 2q sums the
+// first half of node q's run, lane 2q + 1 the second half, each in incidence order, and the even
+// lane adds the two partial sums (first half + second half) and issues the atomics — a fixed order
+// again, with half the loop length and every thread of the CTA busy. `rounds` is uniform over the
+// CTA so that every lane reaches the shuffle. Returns false on a lane whose node sum is out of the
+// fixed-point range.
+#ifndef NFX_FLUSH_PAIRS
+#define NFX_FLUSH_PAIRS 0
+#endif
+template <int TILE>
+__device__ __forceinline__ bool node_flush_pairs(int j, int nn, const uint2* s_node, const unsigned short* inc,
+                                                 const float4* s_cf, const StateDev& s, long long np, float fix_max) {
+    bool ok = true;
+    const int rounds = (2 * nn + TILE - 1) / TILE;
+    for (int r = 0; r < rounds; r++) {
+        const int w = j + r * TILE;
+        float fx = 0.f, fy = 0.f, fz = 0.f;
+        uint2 nd = make_uint2(0u, 0u);
+        if (w < 2 * nn) {
+            nd = s_node[w >> 1];
+            const unsigned first = nd.y >> 16, count = nd.y & 0xffffu, h = (count + 1u) >> 1;
+            const unsigned beg = (w & 1) ? first + h : first, end = (w & 1) ? first + count : first + h;
+            for (unsigned e = beg; e < end; e++) {
+                const float4 c = s_cf[inc[e]];
+                fx += c.x;
+                fy += c.y;
+                fz += c.z;
+            }
+        }
+        const float ox = __shfl_down_sync(0xffffffffu, fx, 1);
+        const float oy = __shfl_down_sync(0xffffffffu, fy, 1);
+        const float oz = __shfl_down_sync(0xffffffffu, fz, 1);
+        if (w < 2 * nn && !(w & 1) && (nd.y & 0xffffu) != 0u) {
+            fx += ox;
+            fy += oy;
+            fz += oz;
+            if (!(fabsf(fx) <= fix_max && fabsf(fy) <= fix_max && fabsf(fz) <= fix_max)) {
+                ok = false;
+            } else {
+                atomicAdd(s.facc + nd.x, (unsigned long long)fix_round(fx * FORCE_FIX_SCALE));
+                atomicAdd(s.facc + np + nd.x, (unsigned long long)fix_round(fy * FORCE_FIX_SCALE));
+                atomicAdd(s.facc + 2 * np + nd.x, (unsigned long long)fix_round(fz * FORCE_FIX_SCALE));
+            }
+        }
+    }
+    return ok;
+}
+
 __device__ __forceinline__ bool clock_bit(const unsigned* mask, int k) { return (mask[k >> 5] >> (k & 31)) & 1u; }
 
 // Sphere centre height, radius and decay rate of an integrated sphere contact for one step.
@@ -324,6 +372,9 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * NFX_TET_REGS))
     __shared__ float4 s_ul[NMAX];
     __shared__ float4 s_cf[4 * TILE];  // corner forces, slot corner*TILE + local tet
     __shared__ ushort4 s_inc[TILE];    // the tile's incidence list
+#if NFX_FLUSH_PAIRS
+    __shared__ uint2 s_node[NMAX];     // the tile's node entries, for the paired flush
+#endif
 #if NFX_DMI_FROM_X
     __shared__ float4 s_xh[NMAX];
     __shared__ float4 s_xl[NMAX];
@@ -367,6 +418,9 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * NFX_TET_REGS))
     uint2 node = make_uint2(0u, 0u);
     if (j < NMAX) {
         node = __ldcs(m.tile_nodes + nb + j);
+#if NFX_FLUSH_PAIRS
+        s_node[j] = node;
+#endif
         const float4 a = s.ua[node.x];
         const float2 lo = s.ub[node.x];
         s_uh[j] = a;  // the law reads x, y, z only
@@ -386,8 +440,14 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * NFX_TET_REGS))
     if (act && element_eval<MODEL, TILE>(j, t, lc, da, db, dc, pa, pb, pc, s_uh, s_ul, s_cf, s, mat, wf))
         raise_status(s, tile_cell_status(bd, b), STATUS_INVERTED);
     __syncthreads();
+#if NFX_FLUSH_PAIRS
+    if (!node_flush_pairs<TILE>(j, nn, s_node, reinterpret_cast<const unsigned short*>(s_inc), s_cf, s, m.np,
+                                m.fix_max))
+        raise_status(s, tile_cell_status(bd, b), STATUS_NONFINITE);
+#else
     if (j < nn && !node_flush<TILE>(node, reinterpret_cast<const unsigned short*>(s_inc), s_cf, s, m.np, m.fix_max))
         raise_status(s, tile_cell_status(bd, b), STATUS_NONFINITE);
+#endif
 }
 
 // Integrated sphere contact (InteractionSphereIntegral.cl), one CTA per tile of a cell that has
