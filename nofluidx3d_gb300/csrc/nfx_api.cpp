@@ -168,14 +168,13 @@ int upload_cell(nfx_sim* s) {
     return NFX_OK;
 }
 
-// Element pass launch: one CTA per tile. pdl: programmatic dependent launch after the previous
-// step's node pass (inside a run of steps only).
-cudaError_t launch_elem(nfx_sim* s, int k, bool pdl = false) {
-    return launch_tet_pass(s->mesh, s->st, table_view(s), s->cell.mat.model, k, s->stream, pdl);
+// Element pass launch: one CTA per tile.
+cudaError_t launch_elem(nfx_sim* s, int k) {
+    return launch_tet_pass(s->mesh, s->st, table_view(s), s->cell.mat.model, k, s->stream);
 }
 
-cudaError_t launch_nodes(nfx_sim* s, int k, int mode, int readout_contact, bool pdl = false) {
-    return launch_node_pass(s->mesh, s->st, table_view(s), s->nblocks, k, mode, readout_contact, s->stream, pdl);
+cudaError_t launch_nodes(nfx_sim* s, int k, int mode, int readout_contact) {
+    return launch_node_pass(s->mesh, s->st, table_view(s), s->nblocks, k, mode, readout_contact, s->stream);
 }
 
 // The integrated sphere contact's own tile pass, when the cell has one.
@@ -191,13 +190,10 @@ cudaError_t prepare_readout(nfx_sim* s, int contact) {
 }
 
 int enqueue_steps(nfx_sim* s, int n) {
-    // The first element pass follows whatever was enqueued before (a kernel writing the plastic
-    // state, say) and is launched in stream order; the later passes overlap their predecessors'
-    // tails (programmatic dependent launch).
     for (int k = 0; k < n; k++) {
-        CUDA_TRY(launch_elem(s, k, k > 0));
+        CUDA_TRY(launch_elem(s, k));
         CUDA_TRY(launch_si(s, k));
-        CUDA_TRY(launch_nodes(s, k, NODE_UPDATE, -1, true));
+        CUDA_TRY(launch_nodes(s, k, NODE_UPDATE, -1));
     }
     CUDA_TRY(launch_advance_time(s->st, n, s->fields_every, s->record_every, s->stream));
     return NFX_OK;
@@ -442,7 +438,6 @@ int nfx_set_mesh(nfx_sim* s, int64_t np, int64_t nt, const double* points, const
     auto& A = s->mesh_allocs;
     int* tb; int* nbg; unsigned* tm; uint2* tn; uchar4* lc; ushort4* ti; float4 *da, *db; float2* dc;
     float4 *xh, *xl, *ua, *va, *bbox; float2 *ub, *vb; unsigned long long* fa; double* part; double* tpart;
-    unsigned* tctr;
     const size_t nblk = (size_t)((np + NODE_BLOCK - 1) / NODE_BLOCK);
     const int64_t ns = P.nslots;
     const size_t ntp = (size_t)ns + ARRAY_PAD;  // per-slot arrays carry ARRAY_PAD zeroed elements
@@ -455,7 +450,6 @@ int nfx_set_mesh(nfx_sim* s, int64_t np, int64_t nt, const double* points, const
         (rc = dalloc(s, &ub, (size_t)np, &A)) || (rc = dalloc(s, &va, (size_t)np, &A)) || (rc = dalloc(s, &vb, (size_t)np, &A)) ||
         (rc = dalloc(s, &fa, 3 * (size_t)np, &A)) || (rc = dalloc(s, &part, (size_t)((np + NODE_BLOCK - 1) / NODE_BLOCK), &A)) ||
         (rc = dalloc(s, &tpart, (size_t)P.ntiles, &A)) || (rc = dalloc(s, &bbox, 2 * nblk, &A)) ||
-        (rc = dalloc(s, &tctr, 2, &A)) ||
         (rc = dalloc(s, &s->d_node_user, (size_t)np, &A)) || (rc = dalloc(s, &s->d_stage, 9 * (size_t)std::max(np, ns), &A))) {
         free_mesh(s);
         return rc;
@@ -494,8 +488,6 @@ int nfx_set_mesh(nfx_sim* s, int64_t np, int64_t nt, const double* points, const
     for (float4* z : {ua, va}) CUDA_TRY(cudaMemsetAsync(z, 0, (size_t)np * sizeof(float4), st));
     for (float2* z : {ub, vb}) CUDA_TRY(cudaMemsetAsync(z, 0, (size_t)np * sizeof(float2), st));
     CUDA_TRY(cudaMemsetAsync(fa, 0, 3 * (size_t)np * sizeof(unsigned long long), st));
-    CUDA_TRY(cudaMemsetAsync(tctr, 0, 2 * sizeof(unsigned), st));
-    CUDA_TRY(prepare_tet_pass());
     CUDA_TRY(cudaMemsetAsync(s->d_clock, 0, sizeof(StepClock), st));
     CUDA_TRY(launch_advance_time(s->st, 0, s->fields_every, s->record_every, st));
     CUDA_TRY(cudaMemsetAsync(s->d_status, 0, sizeof(unsigned), st));
@@ -517,7 +509,6 @@ int nfx_set_mesh(nfx_sim* s, int64_t np, int64_t nt, const double* points, const
     s->mesh.Xl = xl;
     s->mesh.fix_max = P.fix_max;
     s->mesh.block_box = bbox;
-    s->mesh.tile_ctr = tctr;
     s->st.ua = ua;
     s->st.ub = ub;
     s->st.va = va;

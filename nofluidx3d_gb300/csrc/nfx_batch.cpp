@@ -358,15 +358,13 @@ int build_device(nfx_batch* b, const std::vector<int>& which, const std::vector<
         tile_tet_begin[nti] = (int)nt;
         tile_node_begin[nti] = (int)tn_pos;
         int* d_ttb; int* d_tnb; unsigned* d_tm; uint2* d_tn; uchar4* d_lc; ushort4* d_ti; float4 *d_da, *d_db;
-        float2* d_dc; int* d_tc; unsigned* d_ctr;
+        float2* d_dc; int* d_tc;
         float4 *d_pa = nullptr, *d_pb = nullptr; float2 *d_pc = nullptr, *d_fields = nullptr;
         if ((rc = balloc(A, &d_ttb, nti + 1)) || (rc = balloc(A, &d_tnb, nti + 1)) || (rc = balloc(A, &d_tm, nti)) ||
             (rc = balloc(A, &d_tn, ntn + ARRAY_PAD)) || (rc = balloc(A, &d_lc, ntp)) || (rc = balloc(A, &d_ti, ntp)) ||
             (rc = balloc(A, &d_da, ntp)) || (rc = balloc(A, &d_db, ntp)) || (rc = balloc(A, &d_dc, ntp)) ||
-            (rc = balloc(A, &d_tc, nti)) || (rc = balloc(A, &d_ctr, 2)))
+            (rc = balloc(A, &d_tc, nti)))
             return rc;
-        BCUDA(cudaMemsetAsync(d_ctr, 0, 2 * sizeof(unsigned), st));
-        BCUDA(prepare_tet_pass());
         if (b->model == MODEL_VP) {
             if ((rc = balloc(A, &d_pa, ntp)) || (rc = balloc(A, &d_pb, ntp)) || (rc = balloc(A, &d_pc, ntp)) ||
                 (rc = balloc(A, &d_fields, ntp)))
@@ -408,7 +406,6 @@ int build_device(nfx_batch* b, const std::vector<int>& which, const std::vector<
         KM.dmi_a = d_da;
         KM.dmi_b = d_db;
         KM.dmi_c = d_dc;
-        KM.tile_ctr = d_ctr;
         K.st = S;
         K.st.vp_a = d_pa;
         K.st.vp_b = d_pb;
@@ -423,18 +420,13 @@ int build_device(nfx_batch* b, const std::vector<int>& which, const std::vector<
 }
 
 int enqueue_batch_steps(nfx_batch* b, BatchDevice& D, int n) {
-    // Every element pass but the run's first, and every node pass, overlaps its predecessor's tail
-    // (programmatic dependent launch); the first follows whatever was enqueued before in stream
-    // order.
-    bool first = true;
     for (int k = 0; k < n; k++) {
         for (BucketDev& K : D.buckets) {
             if (K.mesh.ntiles <= 0) continue;
-            BCUDA(launch_tet_pass(K.mesh, K.st, K.bd, b->model, k, b->stream, !first));
-            first = false;
+            BCUDA(launch_tet_pass(K.mesh, K.st, K.bd, b->model, k, b->stream));
             if (b->has_si) BCUDA(launch_si_pass(K.mesh, K.st, K.bd, k, false, -1, b->stream));
         }
-        BCUDA(launch_node_pass(D.mesh, D.st, D.bd, D.nblocks, k, NODE_UPDATE, -1, b->stream, true));
+        BCUDA(launch_node_pass(D.mesh, D.st, D.bd, D.nblocks, k, NODE_UPDATE, -1, b->stream));
     }
     BCUDA(launch_advance_time(D.st, n, D.bd.fields_every, D.bd.record_every, b->stream));
     return NFX_OK;

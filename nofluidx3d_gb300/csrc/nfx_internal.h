@@ -107,7 +107,6 @@ struct MeshDev {
     float fix_max;     // per-tile fixed-point bound of the accumulator (force_fix_bound)
     int tile_base;     // index of this launch's first tile in the batch-wide tile numbering
                        // (tile_partials, CellDev::tile_begin/tile_end); 0 for a single cell
-    unsigned* tile_ctr;  // persistent element pass: tile counter and exit count, zero between launches
 };
 
 // Device-side step clock: the simulation time at the start of the current chunk of launches and,
@@ -215,22 +214,14 @@ struct NvtxRange {
 void set_error(const std::string& msg);
 
 // Kernel launchers (nfx_kernels.cu). All enqueue on `stream` and return cudaGetLastError().
-// Element pass over all tiles (one CTA per tile), material from the cell table. pdl: launch with
-// programmatic stream serialisation — only inside a run of steps, where the predecessor is the
-// previous step's node pass or another bucket's element pass (never the first element pass of a
-// run: it may follow any kernel, one that writes the plastic state included).
+// Element pass over all tiles (one CTA per tile), material from the cell table.
 cudaError_t launch_tet_pass(const MeshDev& m, const StateDev& s, const BatchDev& b, int model, int t_offset,
-                            cudaStream_t stream, bool pdl = false);
-// Occupancy of the persistent element pass on the current device; call before the first
-// launch_tet_pass on a device (outside stream capture).
-cudaError_t prepare_tet_pass();
+                            cudaStream_t stream);
 enum NodeMode : int { NODE_UPDATE = 0, NODE_READOUT_ROW = 1, NODE_READOUT_VALUE = 2 };
 // Node pass over `nblocks` node blocks. NODE_READOUT_VALUE sums contact `readout_contact`'s force
 // per cell into force_out[cell] without updating the state.
-// pdl: programmatic stream serialisation, for the NODE_UPDATE pass of a run of steps (its
-// predecessor is an element or integrated-sphere pass, which writes no node state).
 cudaError_t launch_node_pass(const MeshDev& m, const StateDev& s, const BatchDev& b, int nblocks, int t_offset,
-                             int mode, int readout_contact, cudaStream_t stream, bool pdl = false);
+                             int mode, int readout_contact, cudaStream_t stream);
 // Advance the clock by n steps (n = 0: refresh the masks only) for the given schedules.
 cudaError_t launch_advance_time(const StateDev& s, long long n, long long fields_every, long long record_every,
                                 cudaStream_t stream);

@@ -26,31 +26,6 @@
 
 namespace nfx {
 
-// Programmatic dependent launch inside a run of steps. The element and node passes of a step
-// sequence are launched with programmatic stream serialisation (except the sequence's first
-// element pass), so a pass's CTAs are placed on SMs while its predecessor's last CTAs drain and
-// issue their first loads there. Each pass splits at grid_dep_wait(): before it, a pass reads
-// only data that its immediate predecessor does not write; after it, the predecessor has
-// completed and its writes are visible. A pass releases its own dependents (grid_dep_release)
-// only after its wait, so when a pass's CTAs start, the pass two launches back has completed:
-// the data read before the wait was last written at least two launches back. Element pass
-// before its wait: mesh arrays, plastic state, cell table, clock; node pass: displacement,
-// velocity, previous force, reference position, clock, cell table. Launched without the
-// attribute, the wait returns at once (the stream order already holds).
-#ifndef NFX_PDL
-#define NFX_PDL 0
-#endif
-__device__ __forceinline__ void grid_dep_wait() {
-#if NFX_PDL
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-#endif
-}
-__device__ __forceinline__ void grid_dep_release() {
-#if NFX_PDL
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-#endif
-}
-
 __device__ __forceinline__ double contact_pos(const ContactDev& c, long long t) {
     const long long n = c.meta[1];
     if (n > 0) {
@@ -100,27 +75,6 @@ __device__ __forceinline__ bool element_eval(int j, long long t, uchar4 lc, floa
         d[k][0] = (h.x - u0h.x) + (l.x - u0l.x);
         d[k][1] = (h.y - u0h.y) + (l.y - u0l.y);
         d[k][2] = (h.z - u0h.z) + (l.z - u0l.z);
-    }
-    return element_law<MODEL, TILE>(j, t, d, da, db, dc, pa, pb, pc, s_cf, s, mat, write_fields);
-}
-// The same with the tile's displacements staged as the node state's own float4 + float2 words
-// (s_ua[n] = hi x, y, z, lo x; s_ub[n] = lo y, z): the same differences, bit for bit.
-template <int MODEL, int TILE>
-__device__ __forceinline__ bool element_eval_ab(int j, long long t, uchar4 lc, float4 da, float4 db, float2 dc,
-                                                float4 pa, float4 pb, float2 pc, const float4* s_ua,
-                                                const float2* s_ub, float4* s_cf, const StateDev& s,
-                                                const MaterialDev& mat, bool write_fields) {
-    const int li[4] = {lc.x, lc.y, lc.z, lc.w};
-    const float4 a0 = s_ua[li[0]];
-    const float2 b0 = s_ub[li[0]];
-    float d[3][3];
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        const float4 a = s_ua[li[k + 1]];
-        const float2 b = s_ub[li[k + 1]];
-        d[k][0] = (a.x - a0.x) + (a.w - a0.w);
-        d[k][1] = (a.y - a0.y) + (b.x - b0.x);
-        d[k][2] = (a.z - a0.z) + (b.y - b0.y);
     }
     return element_law<MODEL, TILE>(j, t, d, da, db, dc, pa, pb, pc, s_cf, s, mat, write_fields);
 }
@@ -238,54 +192,6 @@ __device__ __forceinline__ bool node_flush(uint2 node, const unsigned short* inc
     atomicAdd(s.facc + np + node.x, (unsigned long long)fix_round(fy * FORCE_FIX_SCALE));
     atomicAdd(s.facc + 2 * np + node.x, (unsigned long long)fix_round(fz * FORCE_FIX_SCALE));
     return true;
-}
-
-// The flush with each tile node's incidence run split over two adjacent lanes: lane 2q sums the
-// first half of node q's run, lane 2q + 1 the second half, each in incidence order, and the even
-// lane adds the two partial sums (first half + second half) and issues the atomics — a fixed order
-// again, with half the loop length and every thread of the CTA busy. `rounds` is uniform over the
-// CTA so that every lane reaches the shuffle. Returns false on a lane whose node sum is out of the
-// fixed-point range.
-#ifndef NFX_FLUSH_PAIRS
-#define NFX_FLUSH_PAIRS 0
-#endif
-template <int TILE>
-__device__ __forceinline__ bool node_flush_pairs(int j, int nn, const uint2* s_node, const unsigned short* inc,
-                                                 const float4* s_cf, const StateDev& s, long long np, float fix_max) {
-    bool ok = true;
-    const int rounds = (2 * nn + TILE - 1) / TILE;
-    for (int r = 0; r < rounds; r++) {
-        const int w = j + r * TILE;
-        float fx = 0.f, fy = 0.f, fz = 0.f;
-        uint2 nd = make_uint2(0u, 0u);
-        if (w < 2 * nn) {
-            nd = s_node[w >> 1];
-            const unsigned first = nd.y >> 16, count = nd.y & 0xffffu, h = (count + 1u) >> 1;
-            const unsigned beg = (w & 1) ? first + h : first, end = (w & 1) ? first + count : first + h;
-            for (unsigned e = beg; e < end; e++) {
-                const float4 c = s_cf[inc[e]];
-                fx += c.x;
-                fy += c.y;
-                fz += c.z;
-            }
-        }
-        const float ox = __shfl_down_sync(0xffffffffu, fx, 1);
-        const float oy = __shfl_down_sync(0xffffffffu, fy, 1);
-        const float oz = __shfl_down_sync(0xffffffffu, fz, 1);
-        if (w < 2 * nn && !(w & 1) && (nd.y & 0xffffu) != 0u) {
-            fx += ox;
-            fy += oy;
-            fz += oz;
-            if (!(fabsf(fx) <= fix_max && fabsf(fy) <= fix_max && fabsf(fz) <= fix_max)) {
-                ok = false;
-            } else {
-                atomicAdd(s.facc + nd.x, (unsigned long long)fix_round(fx * FORCE_FIX_SCALE));
-                atomicAdd(s.facc + np + nd.x, (unsigned long long)fix_round(fy * FORCE_FIX_SCALE));
-                atomicAdd(s.facc + 2 * np + nd.x, (unsigned long long)fix_round(fz * FORCE_FIX_SCALE));
-            }
-        }
-    }
-    return ok;
 }
 
 __device__ __forceinline__ bool clock_bit(const unsigned* mask, int k) { return (mask[k >> 5] >> (k & 31)) & 1u; }
@@ -428,9 +334,6 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * NFX_TET_REGS))
     __shared__ float4 s_ul[NMAX];
     __shared__ float4 s_cf[4 * TILE];  // corner forces, slot corner*TILE + local tet
     __shared__ ushort4 s_inc[TILE];    // the tile's incidence list
-#if NFX_FLUSH_PAIRS
-    __shared__ uint2 s_node[NMAX];     // the tile's node entries, for the paired flush
-#endif
 #if NFX_DMI_FROM_X
     __shared__ float4 s_xh[NMAX];
     __shared__ float4 s_xl[NMAX];
@@ -457,7 +360,6 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * NFX_TET_REGS))
 
     // Streaming per-tetra data (read once per step: evict-first) and the node list, issued for
     // every slot and entry without waiting for the meta word: padding is valid zeroed memory.
-    // Everything up to grid_dep_wait() is data the preceding node pass does not write.
     const uchar4 lc = __ldcs(m.lconn + t);
 #if !NFX_DMI_FROM_X
     const float4 da = __ldcs(m.dmi_a + t);
@@ -473,14 +375,8 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * NFX_TET_REGS))
     }
     s_inc[j] = __ldcs(m.tile_inc + t);
     uint2 node = make_uint2(0u, 0u);
-    if (j < NMAX) node = __ldcs(m.tile_nodes + nb + j);
-    const MaterialDev mat = bd.cells[bd.tile_cell ? __ldg(bd.tile_cell + b) : 0].mat;
-    grid_dep_wait();  // displacements written and the accumulator cleared by the node pass
-    grid_dep_release();
     if (j < NMAX) {
-#if NFX_FLUSH_PAIRS
-        s_node[j] = node;
-#endif
+        node = __ldcs(m.tile_nodes + nb + j);
         const float4 a = s.ua[node.x];
         const float2 lo = s.ub[node.x];
         s_uh[j] = a;  // the law reads x, y, z only
@@ -490,6 +386,7 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * NFX_TET_REGS))
         s_xl[j] = m.Xl[node.x];
 #endif
     }
+    const MaterialDev mat = bd.cells[bd.tile_cell ? __ldg(bd.tile_cell + b) : 0].mat;
     __syncthreads();
 #if NFX_DMI_FROM_X
     float4 da = make_float4(0.f, 0.f, 0.f, 0.f), db = da;
@@ -499,166 +396,8 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * NFX_TET_REGS))
     if (act && element_eval<MODEL, TILE>(j, t, lc, da, db, dc, pa, pb, pc, s_uh, s_ul, s_cf, s, mat, wf))
         raise_status(s, tile_cell_status(bd, b), STATUS_INVERTED);
     __syncthreads();
-#if NFX_FLUSH_PAIRS
-    if (!node_flush_pairs<TILE>(j, nn, s_node, reinterpret_cast<const unsigned short*>(s_inc), s_cf, s, m.np,
-                                m.fix_max))
-        raise_status(s, tile_cell_status(bd, b), STATUS_NONFINITE);
-#else
     if (j < nn && !node_flush<TILE>(node, reinterpret_cast<const unsigned short*>(s_inc), s_cf, s, m.np, m.fix_max))
         raise_status(s, tile_cell_status(bd, b), STATUS_NONFINITE);
-#endif
-}
-
-// ------------------------------------------------------------------------------------------
-// Element pass, persistent and software-pipelined (tiles of 128 tetrahedra)
-// ------------------------------------------------------------------------------------------
-// A grid of as many CTAs as fit on the GPU at once; each CTA takes tiles from a counter and,
-// while it evaluates one tile, has the next tile's per-tetra data (local connectivity, Dm^-1 and
-// V0, plastic state, incidence list, node list) on its way into shared memory by cp.async, and
-// gathers the next tile's node displacements while it flushes the current tile's forces. The
-// same arithmetic as k_tet_pass in the same per-tile order, so results are identical bit for bit;
-// only the assignment of tiles to CTAs differs, which the integer accumulator does not see.
-//
-// Tile order: CTA c takes tile index c first, then indices G, G+1, ... from the counter (G = grid
-// size), tile b = ntiles-1-index (serpentine with the node pass, as k_tet_pass). The counter
-// (tile_ctr[0]) and the exit count (tile_ctr[1]) are zero at launch; the last CTA to finish sets
-// both back to zero, after every CTA has made its last fetch.
-#ifndef NFX_TET_PERSIST
-#define NFX_TET_PERSIST 0
-#endif
-constexpr int PERSIST_TILE = 128;
-constexpr int PERSIST_CTAS_PER_SM = 8;  // shared memory: about 27 KB per CTA
-
-__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void cpa16(void* d, const void* g) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(d)), "l"(g) : "memory");
-}
-__device__ __forceinline__ void cpa8(void* d, const void* g) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_addr(d)), "l"(g) : "memory");
-}
-__device__ __forceinline__ void cpa4(void* d, const void* g) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(d)), "l"(g) : "memory");
-}
-__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cpa_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
-
-template <int MODEL>
-__global__ void __launch_bounds__(PERSIST_TILE, PERSIST_CTAS_PER_SM)
-    k_tet_pass_p(MeshDev m, StateDev s, BatchDev bd, int t_offset) {
-    constexpr int TILE = PERSIST_TILE;
-    constexpr int NMAX = TILE < TILE_NODES_MAX ? TILE : TILE_NODES_MAX;
-    // node displacements of the current tile (the node state's own words)
-    __shared__ float4 s_ua[NMAX];
-    __shared__ float2 s_ub[NMAX];
-    __shared__ float4 s_cf[4 * TILE];  // corner forces, slot corner*TILE + local tet
-    // per-tetra stage: slot j is filled and read by thread j only
-    __shared__ float4 s_da[TILE], s_db[TILE], s_pa[TILE], s_pb[TILE];
-    __shared__ float2 s_dc[TILE], s_pc[TILE];
-    __shared__ uchar4 s_lc[TILE];
-    // read across threads in the flush: double-buffered
-    __shared__ ushort4 s_inc[2][TILE];
-    __shared__ uint2 s_node[2][NMAX];
-    __shared__ unsigned s_meta[2];
-    __shared__ int s_next;
-
-    const int j = threadIdx.x;
-    const int G = (int)gridDim.x, ntiles = m.ntiles;
-    unsigned* ctr = m.tile_ctr;
-    auto tile_of = [&](int idx) { return NFX_TILE_REVERSE ? ntiles - 1 - idx : idx; };
-    // this thread's copies of tile b's slot j (and node entry j, and the meta word) into buffer q
-    auto stage = [&](int b, int q) {
-        const long long t = (long long)b * TILE + j;
-        cpa4(&s_lc[j], m.lconn + t);
-        cpa16(&s_da[j], m.dmi_a + t);
-        cpa16(&s_db[j], m.dmi_b + t);
-        cpa8(&s_dc[j], m.dmi_c + t);
-        if (MODEL == MODEL_VP) {
-            cpa16(&s_pa[j], s.vp_a + t);
-            cpa16(&s_pb[j], s.vp_b + t);
-            cpa8(&s_pc[j], s.vp_c + t);
-        }
-        cpa8(&s_inc[q][j], m.tile_inc + t);
-        if (j < NMAX) cpa8(&s_node[q][j], m.tile_nodes + (long long)b * NMAX + j);
-        if (j == 0) cpa4(&s_meta[q], m.tile_meta + b);
-        cpa_commit();
-    };
-    // the tile's node displacements (entries of buffer q), issued by thread j for node entry j
-    auto gather = [&](int q, int nn) {
-        if (j < nn) {
-            const unsigned id = s_node[q][j].x;
-            cpa16(&s_ua[j], s.ua + id);
-            cpa8(&s_ub[j], s.ub + id);
-        }
-        cpa_commit();
-    };
-
-    int b = tile_of(blockIdx.x);
-    stage(b, 0);  // mesh arrays and plastic state: not written by the preceding node pass
-    grid_dep_wait();
-    grid_dep_release();
-    const bool wf = clock_bit(s.clock->fields_due, t_offset);
-    int fetched = j == 0 ? G + (int)atomicAdd(ctr, 1u) : 0;
-    cpa_wait_all();
-    __syncthreads();
-    unsigned meta = s_meta[0];
-    gather(0, (int)(meta >> 16));
-    uchar4 lc = s_lc[j];
-    float4 da = s_da[j], db = s_db[j], pa = make_float4(0.f, 0.f, 0.f, 0.f), pb = pa;
-    float2 dc = s_dc[j], pc = make_float2(0.f, 0.f);
-    if (MODEL == MODEL_VP) {
-        pa = s_pa[j];
-        pb = s_pb[j];
-        pc = s_pc[j];
-    }
-    if (j == 0) s_next = fetched;
-    cpa_wait_all();
-    __syncthreads();
-    int q = 0;
-    for (;;) {
-        const int nidx = s_next;
-        const bool more = nidx < ntiles;  // uniform over the CTA
-        if (more) stage(tile_of(nidx), q ^ 1);
-        if (j == 0 && more) fetched = G + (int)atomicAdd(ctr, 1u);
-        const MaterialDev mat = bd.cells[bd.tile_cell ? __ldg(bd.tile_cell + b) : 0].mat;
-        const int ntt = (int)(meta & 0xffffu), nn = (int)(meta >> 16);
-        if (j < ntt &&
-            element_eval_ab<MODEL, TILE>(j, (long long)b * TILE + j, lc, da, db, dc, pa, pb, pc, s_ua, s_ub, s_cf,
-                                         s, mat, wf))
-            raise_status(s, tile_cell_status(bd, b), STATUS_INVERTED);
-        if (more) cpa_wait_all();
-        __syncthreads();  // corner forces complete; the next tile's stage in place
-        unsigned nmeta = 0u;
-        if (more) {
-            nmeta = s_meta[q ^ 1];
-            gather(q ^ 1, (int)(nmeta >> 16));
-        }
-        if (j < nn &&
-            !node_flush<TILE>(s_node[q][j], reinterpret_cast<const unsigned short*>(s_inc[q]), s_cf, s, m.np, m.fix_max))
-            raise_status(s, tile_cell_status(bd, b), STATUS_NONFINITE);
-        if (more) {
-            lc = s_lc[j];
-            da = s_da[j];
-            db = s_db[j];
-            dc = s_dc[j];
-            if (MODEL == MODEL_VP) {
-                pa = s_pa[j];
-                pb = s_pb[j];
-                pc = s_pc[j];
-            }
-        }
-        if (j == 0) s_next = more ? fetched : ntiles;
-        cpa_wait_all();
-        __syncthreads();  // the next tile's displacements in place; s_cf and buffer q free
-        if (!more) break;
-        b = tile_of(nidx);
-        meta = nmeta;
-        q ^= 1;
-    }
-    // every fetch of this CTA is done: the last CTA out resets the counters for the next launch
-    if (j == 0 && atomicAdd(ctr + 1, 1u) == (unsigned)(G - 1)) {
-        ctr[0] = 0u;
-        ctr[1] = 0u;
-    }
 }
 
 // Integrated sphere contact (InteractionSphereIntegral.cl), one CTA per tile of a cell that has
@@ -845,31 +584,20 @@ __device__ __forceinline__ bool contact_force(const ContactDev& c, const WallSte
     return true;
 }
 
-// One node, in two halves around the node pass's grid_dep_wait(). node_load reads what the
-// element pass does not write: the displacement hi/lo and, in a block near a contact, the
-// reference position. node_finish adds the
-// element force from the fixed-point accumulator and the contacts in order (returning the y force
-// of contact rc on the node; the readout is minus its sum, negated once per cell so that no node
-// runs a double negation), and in update mode runs the cell's integrator with the displacement
-// carried as hi + lo — damped velocity Verlet with unit mass and the FIXED_TOP_BOTTOM pin
-// (VelocityVerlet.cl), or the lumped-mass form (velocityVerlet2.cl) — and resets the accumulator.
-#ifndef NFX_NODE_EARLY
-#define NFX_NODE_EARLY 0  // 1: node_load before the node pass's wait (48 bytes of spills at 64 registers)
-#endif
-#ifndef NFX_NODE_EARLY_V
-#define NFX_NODE_EARLY_V 0  // 1: velocity and previous force also read in node_load
-#endif
+// One node, in two halves. node_load reads the displacement hi/lo and, in a block near a
+// contact, the reference position. node_finish adds the element force from the fixed-point
+// accumulator and the contacts in order (returning the y force of contact rc on the node; the
+// readout is minus its sum, negated once per cell so that no node runs a double negation), and in
+// update mode runs the cell's integrator with the displacement carried as hi + lo — damped
+// velocity Verlet with unit mass and the FIXED_TOP_BOTTOM pin (VelocityVerlet.cl), or the
+// lumped-mass form (velocityVerlet2.cl) — and resets the accumulator.
 struct NodeLoad {
     float4 xh, a;  // reference position (when loaded), displacement hi + u_lo.x
     float2 lo;     // u_lo.yz
-#if NFX_NODE_EARLY_V
-    float4 va;
-    float2 vb;
-#endif
     bool xh_loaded;
 };
 __device__ __forceinline__ NodeLoad node_load(const MeshDev& m, const StateDev& s, int i, bool near,
-                                              const CellDev& C, bool update) {
+                                              const CellDev& C) {
     NodeLoad r;
     // In a block near a contact (or under the lumped-mass integrator, which needs Xh.w) the
     // reference position is read with the node's first loads; elsewhere only after the per-node
@@ -879,15 +607,6 @@ __device__ __forceinline__ NodeLoad node_load(const MeshDev& m, const StateDev& 
     if (r.xh_loaded) r.xh = m.Xh[i];
     r.a = s.ua[i];
     r.lo = s.ub[i];
-#if NFX_NODE_EARLY_V
-    // velocity and previous force: streamed once per step (evict-first)
-    r.va = make_float4(0.f, 0.f, 0.f, 0.f);
-    r.vb = make_float2(0.f, 0.f);
-    if (update) {
-        r.va = __ldcs(s.va + i);
-        r.vb = __ldcs(s.vb + i);
-    }
-#endif
     return r;
 }
 
@@ -913,14 +632,9 @@ __device__ __forceinline__ double node_finish(const MeshDev& m, const StateDev& 
         if (((reach >> c) & 1u) && contact_force(cs[c], wall[c], xh, m.Xl + i, uh, ul, f, fy) && c == rc) fy_rc = fy;
     }
     if (!update) return fy_rc;
-#if NFX_NODE_EARLY_V
-    const float4 va = L.va;
-    const float2 vb = L.vb;
-#else
     // velocity and previous force: streamed once per step (evict-first)
     const float4 va = __ldcs(s.va + i);
     const float2 vb = __ldcs(s.vb + i);
-#endif
     float3 v = make_float3(va.x, va.y, va.z);
     float3 nf;  // the new previous-force slot
     if (C.integrator == INTEGRATOR_VV2) {
@@ -991,14 +705,6 @@ __global__ void __launch_bounds__(NODE_BLOCK, NFX_NODE_MIN_BLOCKS) k_node_pass(M
     }
     if (threadIdx.x >= 32 && threadIdx.x < 34) s_box[threadIdx.x - 32] = m.block_box[2 * blockIdx.x + (threadIdx.x - 32)];
     __syncthreads();
-#if NFX_NODE_EARLY
-    // the node's displacement (and reference position near a contact) before the wait
-    const bool near = !NFX_NODE_CULL || block_near(C.c, C.n_contacts, s_wall, s_box[0], s_box[1]);
-    NodeLoad L;
-    if (i < C.node_end) L = node_load(m, s, i, near, C, mode == NODE_UPDATE);
-#endif
-    grid_dep_wait();  // the element pass's forces in the accumulator (and its tile partials)
-    grid_dep_release();
     int rc;
     bool rec;
     long long row = 0;
@@ -1019,12 +725,8 @@ __global__ void __launch_bounds__(NODE_BLOCK, NFX_NODE_MIN_BLOCKS) k_node_pass(M
     double fy = 0.0;  // y force of the readout contact on this node
     const bool update = mode == NODE_UPDATE;
     unsigned* cstat = bd.cell_status ? bd.cell_status + cell : nullptr;
-#if NFX_NODE_EARLY
-    if (i < C.node_end) fy = node_finish(m, s, i, s_wall, s_box, L, C, rc, update, cstat);
-#else
     const bool near = !NFX_NODE_CULL || block_near(C.c, C.n_contacts, s_wall, s_box[0], s_box[1]);
-    if (i < C.node_end) fy = node_finish(m, s, i, s_wall, s_box, node_load(m, s, i, near, C, update), C, rc, update, cstat);
-#endif
+    if (i < C.node_end) fy = node_finish(m, s, i, s_wall, s_box, node_load(m, s, i, near, C), C, rc, update, cstat);
     if (!rec) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     fy = warp_sum_d(fy);
@@ -1158,96 +860,28 @@ __global__ void k_vec_from_user(int np, float4* a, float2* b, int part, const lo
 // ------------------------------------------------------------------------------------------
 // Launchers
 // ------------------------------------------------------------------------------------------
-// A launch with programmatic stream serialisation when `pdl` is set (the kernel may start while
-// its predecessor in the stream drains; see grid_dep_wait), a plain stream-ordered one otherwise.
-template <typename... KArgs, typename... Args>
-static cudaError_t launch_k(void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStream_t st, bool pdl, Args... args) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = grid;
-    cfg.blockDim = block;
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = (NFX_PDL && pdl) ? 1 : 0;
-    return cudaLaunchKernelEx(&cfg, kern, args...);
-}
-
 template <int TILE>
 static cudaError_t launch_tile(const MeshDev& m, const StateDev& s, const BatchDev& b, int model, int t_offset,
-                               cudaStream_t st, bool pdl) {
+                               cudaStream_t st) {
     const dim3 grid((unsigned)m.ntiles), block(TILE);
     switch (model) {
-        case MODEL_MR: return launch_k(k_tet_pass<MODEL_MR, TILE>, grid, block, st, pdl, m, s, b, t_offset);
-        case MODEL_SVK: return launch_k(k_tet_pass<MODEL_SVK, TILE>, grid, block, st, pdl, m, s, b, t_offset);
-        case MODEL_SVKK: return launch_k(k_tet_pass<MODEL_SVKK, TILE>, grid, block, st, pdl, m, s, b, t_offset);
-        case MODEL_VP: return launch_k(k_tet_pass<MODEL_VP, TILE>, grid, block, st, pdl, m, s, b, t_offset);
+        case MODEL_MR: k_tet_pass<MODEL_MR, TILE><<<grid, block, 0, st>>>(m, s, b, t_offset); break;
+        case MODEL_SVK: k_tet_pass<MODEL_SVK, TILE><<<grid, block, 0, st>>>(m, s, b, t_offset); break;
+        case MODEL_SVKK: k_tet_pass<MODEL_SVKK, TILE><<<grid, block, 0, st>>>(m, s, b, t_offset); break;
+        case MODEL_VP: k_tet_pass<MODEL_VP, TILE><<<grid, block, 0, st>>>(m, s, b, t_offset); break;
         default: return cudaErrorInvalidValue;
     }
-}
-
-// Resident CTAs of the persistent element pass per SM, and SMs, per device ordinal (filled by
-// prepare_tet_pass before any launch, outside stream capture).
-static int g_persist_occ[64][4], g_persist_sms[64];
-
-template <int MODEL>
-static cudaError_t persist_occupancy(int& occ) {
-    cudaError_t e = cudaFuncSetAttribute(k_tet_pass_p<MODEL>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                         (int)cudaSharedmemCarveoutMaxShared);
-    if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_tet_pass_p<MODEL>, PERSIST_TILE, 0);
-}
-
-cudaError_t prepare_tet_pass() {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-    if (!NFX_TET_PERSIST || g_persist_sms[dev] > 0) return cudaSuccess;
-    int o[4] = {0, 0, 0, 0}, n = 0;
-    if ((e = persist_occupancy<MODEL_MR>(o[MODEL_MR])) != cudaSuccess) return e;
-    if ((e = persist_occupancy<MODEL_SVK>(o[MODEL_SVK])) != cudaSuccess) return e;
-    if ((e = persist_occupancy<MODEL_SVKK>(o[MODEL_SVKK])) != cudaSuccess) return e;
-    if ((e = persist_occupancy<MODEL_VP>(o[MODEL_VP])) != cudaSuccess) return e;
-    if ((e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    for (int k = 0; k < 4; k++) g_persist_occ[dev][k] = o[k];
-    g_persist_sms[dev] = n;
-    return cudaSuccess;
-}
-
-// The persistent element pass: grid = resident CTAs on this device (at most one per tile).
-template <int MODEL>
-static cudaError_t launch_persist(const MeshDev& m, const StateDev& s, const BatchDev& b, int t_offset,
-                                  cudaStream_t st, bool pdl) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= 64 || g_persist_sms[dev] <= 0 || g_persist_occ[dev][MODEL] <= 0)
-        return cudaErrorNotReady;  // prepare_tet_pass was not called on this device
-    const long long cap = (long long)g_persist_occ[dev][MODEL] * g_persist_sms[dev];
-    const unsigned grid = (unsigned)(m.ntiles < cap ? m.ntiles : cap);
-    return launch_k(k_tet_pass_p<MODEL>, dim3(grid), dim3(PERSIST_TILE), st, pdl, m, s, b, t_offset);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_tet_pass(const MeshDev& m, const StateDev& s, const BatchDev& b, int model, int t_offset,
-                            cudaStream_t st, bool pdl) {
+                            cudaStream_t st) {
     if (m.ntiles <= 0) return cudaSuccess;
-    if (NFX_TET_PERSIST && m.tile_tets == PERSIST_TILE && m.tile_ctr) {
-        switch (model) {
-            case MODEL_MR: return launch_persist<MODEL_MR>(m, s, b, t_offset, st, pdl);
-            case MODEL_SVK: return launch_persist<MODEL_SVK>(m, s, b, t_offset, st, pdl);
-            case MODEL_SVKK: return launch_persist<MODEL_SVKK>(m, s, b, t_offset, st, pdl);
-            case MODEL_VP: return launch_persist<MODEL_VP>(m, s, b, t_offset, st, pdl);
-            default: return cudaErrorInvalidValue;
-        }
-    }
     switch (m.tile_tets) {
-        case 64: return launch_tile<64>(m, s, b, model, t_offset, st, pdl);
-        case 128: return launch_tile<128>(m, s, b, model, t_offset, st, pdl);
-        case 256: return launch_tile<256>(m, s, b, model, t_offset, st, pdl);
-        case 512: return launch_tile<512>(m, s, b, model, t_offset, st, pdl);
+        case 64: return launch_tile<64>(m, s, b, model, t_offset, st);
+        case 128: return launch_tile<128>(m, s, b, model, t_offset, st);
+        case 256: return launch_tile<256>(m, s, b, model, t_offset, st);
+        case 512: return launch_tile<512>(m, s, b, model, t_offset, st);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -1267,10 +901,10 @@ cudaError_t launch_si_pass(const MeshDev& m, const StateDev& s, const BatchDev& 
 }
 
 cudaError_t launch_node_pass(const MeshDev& m, const StateDev& s, const BatchDev& b, int nblocks, int t_offset,
-                             int mode, int readout_contact, cudaStream_t st, bool pdl) {
+                             int mode, int readout_contact, cudaStream_t st) {
     if (nblocks <= 0) return cudaSuccess;
-    return launch_k(k_node_pass, dim3((unsigned)nblocks), dim3(NODE_BLOCK), st, pdl, m, s, b, t_offset, mode,
-                    readout_contact);
+    k_node_pass<<<nblocks, NODE_BLOCK, 0, st>>>(m, s, b, t_offset, mode, readout_contact);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_advance_time(const StateDev& s, long long n, long long fields_every, long long record_every,
