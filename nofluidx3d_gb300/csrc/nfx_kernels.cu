@@ -326,12 +326,42 @@ __device__ __forceinline__ void ref_shape_inverse(uchar4 lc, const float4* s_xh,
     db = make_float4(A4 * r, A5 * r, A6 * r, A7 * r);
     dc = make_float2(A8 * r, det * (1.0f / 6.0f));
 }
+// Tile-relative displacements: the element pass stages, per tile node, the displacement minus
+// that of the tile's first node, (h - h_ref) + (l - l_ref) per component with u = h + l (hi/lo),
+// in one float4 — a quantity of the size of the tile's deformation, which FP32 holds to the
+// accuracy the hi/lo pair gives the differences — and a tetrahedron's edge differences are
+// v_k - v_0. Against staging hi and lo (two float4 per node, and per corner two shared loads and
+// nine additions), this halves the shared-memory traffic of the gather, the pass's busiest unit.
+#ifndef NFX_TILE_REL
+#define NFX_TILE_REL 1
+#endif
+template <int MODEL, int TILE>
+__device__ __forceinline__ bool element_eval_rel(int j, long long t, uchar4 lc, float4 da, float4 db, float2 dc,
+                                                 float4 pa, float4 pb, float2 pc, const float4* s_v, float4* s_cf,
+                                                 const StateDev& s, const MaterialDev& mat, bool write_fields) {
+    const int li[4] = {lc.x, lc.y, lc.z, lc.w};
+    const float4 v0 = s_v[li[0]];
+    float d[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const float4 v = s_v[li[k + 1]];
+        d[k][0] = v.x - v0.x;
+        d[k][1] = v.y - v0.y;
+        d[k][2] = v.z - v0.z;
+    }
+    return element_law<MODEL, TILE>(j, t, d, da, db, dc, pa, pb, pc, s_cf, s, mat, write_fields);
+}
+
 template <int MODEL, int TILE>
 __global__ void __launch_bounds__(TILE, 65536 / (TILE * NFX_TET_REGS))
     k_tet_pass(MeshDev m, StateDev s, BatchDev bd, int t_offset) {
     constexpr int NMAX = TILE < TILE_NODES_MAX ? TILE : TILE_NODES_MAX;
+#if NFX_TILE_REL
+    __shared__ float4 s_v[NMAX];  // tile-relative displacement of each tile node (x, y, z)
+#else
     __shared__ float4 s_uh[NMAX];
     __shared__ float4 s_ul[NMAX];
+#endif
     __shared__ float4 s_cf[4 * TILE];  // corner forces, slot corner*TILE + local tet
     __shared__ ushort4 s_inc[TILE];    // the tile's incidence list
 #if NFX_DMI_FROM_X
@@ -375,12 +405,23 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * NFX_TET_REGS))
     }
     s_inc[j] = __ldcs(m.tile_inc + t);
     uint2 node = make_uint2(0u, 0u);
+#if NFX_TILE_REL
+    // the tile's first node (every thread loads the same words: one broadcast transaction)
+    const unsigned ref = __ldg(&m.tile_nodes[nb].x);
+    const float4 ar = s.ua[ref];
+    const float2 lr = s.ub[ref];
+#endif
     if (j < NMAX) {
         node = __ldcs(m.tile_nodes + nb + j);
         const float4 a = s.ua[node.x];
         const float2 lo = s.ub[node.x];
+#if NFX_TILE_REL
+        s_v[j] = make_float4((a.x - ar.x) + (a.w - ar.w), (a.y - ar.y) + (lo.x - lr.x), (a.z - ar.z) + (lo.y - lr.y),
+                             0.f);
+#else
         s_uh[j] = a;  // the law reads x, y, z only
         s_ul[j] = make_float4(a.w, lo.x, lo.y, 0.f);
+#endif
 #if NFX_DMI_FROM_X
         s_xh[j] = m.Xh[node.x];
         s_xl[j] = m.Xl[node.x];
@@ -393,8 +434,13 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * NFX_TET_REGS))
     float2 dc = make_float2(0.f, 0.f);
     if (act) ref_shape_inverse(lc, s_xh, s_xl, da, db, dc);
 #endif
+#if NFX_TILE_REL
+    if (act && element_eval_rel<MODEL, TILE>(j, t, lc, da, db, dc, pa, pb, pc, s_v, s_cf, s, mat, wf))
+        raise_status(s, tile_cell_status(bd, b), STATUS_INVERTED);
+#else
     if (act && element_eval<MODEL, TILE>(j, t, lc, da, db, dc, pa, pb, pc, s_uh, s_ul, s_cf, s, mat, wf))
         raise_status(s, tile_cell_status(bd, b), STATUS_INVERTED);
+#endif
     __syncthreads();
     if (j < nn && !node_flush<TILE>(node, reinterpret_cast<const unsigned short*>(s_inc), s_cf, s, m.np, m.fix_max))
         raise_status(s, tile_cell_status(bd, b), STATUS_NONFINITE);
