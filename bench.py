@@ -473,8 +473,11 @@ def main():
     # that a short timed region still has clock samples under load around it.
     clocks = ClockSampler(local)
     clocks.start()
+    # the window stays within the workload's own duration (w.steps), so that the cell is still in
+    # its physical range when the timed steps and the e2e intervals that follow run
     window_ms = 0.0
-    while window_ms < 1e3 * args.clock_window_s:
+    after = args.steps + args.profile_steps + args.e2e_steps + 400
+    while window_ms < 1e3 * args.clock_window_s and sim.time + 1000 + after <= w.steps:
         window_ms += sim.time_steps(1000)
     barrier(dist, local)
     ms = sim.time_steps(args.steps)
