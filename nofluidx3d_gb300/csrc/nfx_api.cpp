@@ -173,8 +173,8 @@ cudaError_t launch_elem(nfx_sim* s, int k) {
     return launch_tet_pass(s->mesh, s->st, table_view(s), s->cell.mat.model, k, s->stream);
 }
 
-cudaError_t launch_nodes(nfx_sim* s, int k, int mode, int readout_contact) {
-    return launch_node_pass(s->mesh, s->st, table_view(s), s->nblocks, k, mode, readout_contact, s->stream);
+cudaError_t launch_nodes(nfx_sim* s, int k, int mode, int readout_contact, bool pdl = false) {
+    return launch_node_pass(s->mesh, s->st, table_view(s), s->nblocks, k, mode, readout_contact, s->stream, pdl);
 }
 
 // The integrated sphere contact's own tile pass, when the cell has one.
@@ -193,7 +193,7 @@ int enqueue_steps(nfx_sim* s, int n) {
     for (int k = 0; k < n; k++) {
         CUDA_TRY(launch_elem(s, k));
         CUDA_TRY(launch_si(s, k));
-        CUDA_TRY(launch_nodes(s, k, NODE_UPDATE, -1));
+        CUDA_TRY(launch_nodes(s, k, NODE_UPDATE, -1, true));  // programmatic dependent launch
     }
     CUDA_TRY(launch_advance_time(s->st, n, s->fields_every, s->record_every, s->stream));
     return NFX_OK;

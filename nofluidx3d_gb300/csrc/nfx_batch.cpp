@@ -426,7 +426,7 @@ int enqueue_batch_steps(nfx_batch* b, BatchDevice& D, int n) {
             BCUDA(launch_tet_pass(K.mesh, K.st, K.bd, b->model, k, b->stream));
             if (b->has_si) BCUDA(launch_si_pass(K.mesh, K.st, K.bd, k, false, -1, b->stream));
         }
-        BCUDA(launch_node_pass(D.mesh, D.st, D.bd, D.nblocks, k, NODE_UPDATE, -1, b->stream));
+        BCUDA(launch_node_pass(D.mesh, D.st, D.bd, D.nblocks, k, NODE_UPDATE, -1, b->stream, true));
     }
     BCUDA(launch_advance_time(D.st, n, D.bd.fields_every, D.bd.record_every, b->stream));
     return NFX_OK;

@@ -220,8 +220,10 @@ cudaError_t launch_tet_pass(const MeshDev& m, const StateDev& s, const BatchDev&
 enum NodeMode : int { NODE_UPDATE = 0, NODE_READOUT_ROW = 1, NODE_READOUT_VALUE = 2 };
 // Node pass over `nblocks` node blocks. NODE_READOUT_VALUE sums contact `readout_contact`'s force
 // per cell into force_out[cell] without updating the state.
+// pdl: programmatic dependent launch, for the NODE_UPDATE pass of a run of steps only (its
+// predecessor then is an element or integrated-sphere pass, launched in plain stream order).
 cudaError_t launch_node_pass(const MeshDev& m, const StateDev& s, const BatchDev& b, int nblocks, int t_offset,
-                             int mode, int readout_contact, cudaStream_t stream);
+                             int mode, int readout_contact, cudaStream_t stream, bool pdl = false);
 // Advance the clock by n steps (n = 0: refresh the masks only) for the given schedules.
 cudaError_t launch_advance_time(const StateDev& s, long long n, long long fields_every, long long record_every,
                                 cudaStream_t stream);

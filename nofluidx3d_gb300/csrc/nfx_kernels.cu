@@ -26,6 +26,25 @@
 
 namespace nfx {
 
+// Programmatic dependent launch of the node pass. Inside a run of steps the node pass is launched
+// with programmatic stream serialisation (NFX_PDL_NODE), so its CTAs can be placed on the SMs
+// before the element pass has completed: a node-pass CTA computes its prologue (the cell's
+// contact positions from the step clock and the cell table, its block's reference box — data the
+// element pass does not write, last written by work that completed before the element pass
+// started), then waits in griddepcontrol.wait until the element pass has completed and its
+// writes are visible, and only then touches the node state. The element pass itself is launched
+// in plain stream order and, with NFX_TET_TRIGGER, allows its dependents to launch as soon as each
+// of its CTAs starts (launch_dependents), so that node-pass CTAs take the SMs its last CTAs leave.
+// A kernel launched without the attribute passes the wait at once.
+#ifndef NFX_PDL_NODE
+#define NFX_PDL_NODE 1
+#endif
+#ifndef NFX_TET_TRIGGER
+#define NFX_TET_TRIGGER 1
+#endif
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ double contact_pos(const ContactDev& c, long long t) {
     const long long n = c.meta[1];
     if (n > 0) {
@@ -378,6 +397,9 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * NFX_TET_REGS))
 #endif
     const int b = NFX_TILE_REVERSE ? (int)(gridDim.x - 1 - blockIdx.x) : (int)blockIdx.x;
     const int j = threadIdx.x;
+#if NFX_TET_TRIGGER
+    if (j == 0) grid_dep_trigger();
+#endif
     // fixed-stride tiles: the tile's slots and node entries are addressed without a load; the
     // real counts come from the tile's meta word (loaded alongside the data)
     const int t = b * TILE + j;
@@ -751,6 +773,9 @@ __global__ void __launch_bounds__(NODE_BLOCK, NFX_NODE_MIN_BLOCKS) k_node_pass(M
     }
     if (threadIdx.x >= 32 && threadIdx.x < 34) s_box[threadIdx.x - 32] = m.block_box[2 * blockIdx.x + (threadIdx.x - 32)];
     __syncthreads();
+#if NFX_PDL_NODE
+    grid_dep_wait();  // the element pass's forces in the accumulator
+#endif
     int rc;
     bool rec;
     long long row = 0;
@@ -947,10 +972,18 @@ cudaError_t launch_si_pass(const MeshDev& m, const StateDev& s, const BatchDev& 
 }
 
 cudaError_t launch_node_pass(const MeshDev& m, const StateDev& s, const BatchDev& b, int nblocks, int t_offset,
-                             int mode, int readout_contact, cudaStream_t st) {
+                             int mode, int readout_contact, cudaStream_t st, bool pdl) {
     if (nblocks <= 0) return cudaSuccess;
-    k_node_pass<<<nblocks, NODE_BLOCK, 0, st>>>(m, s, b, t_offset, mode, readout_contact);
-    return cudaGetLastError();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)nblocks);
+    cfg.blockDim = dim3(NODE_BLOCK);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = (NFX_PDL_NODE && pdl) ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k_node_pass, m, s, b, t_offset, mode, readout_contact);
 }
 
 cudaError_t launch_advance_time(const StateDev& s, long long n, long long fields_every, long long record_every,
