@@ -184,38 +184,12 @@ __device__ __forceinline__ float fix_to_float(unsigned long long w) {
 #ifndef NFX_FLUSH_UNROLL
 #define NFX_FLUSH_UNROLL 1
 #endif
-#ifndef NFX_FLUSH_INC4
-#define NFX_FLUSH_INC4 1  // 0: one shared load per incidence entry
-#endif
 template <int TILE>
 __device__ __forceinline__ bool node_flush(uint2 node, const unsigned short* inc, const float4* s_cf,
                                            const StateDev& s, long long np, float fix_max) {
     const unsigned first = node.y >> 16, count = node.y & 0xffffu;
     if (count == 0) return true;
     float fx = 0.f, fy = 0.f, fz = 0.f;
-#if NFX_FLUSH_INC4
-    // The run's incidence entries read four at a time (aligned 8-byte loads of the list), each
-    // entry still added in list order: one shared load per four entries instead of one per entry.
-    {
-        const uint2* inc4 = reinterpret_cast<const uint2*>(inc);
-        const unsigned end = first + count;
-        for (unsigned c = first >> 2; c <= (end - 1) >> 2; c++) {
-            const uint2 w = inc4[c];
-            const unsigned short e4[4] = {(unsigned short)(w.x & 0xffffu), (unsigned short)(w.x >> 16),
-                                          (unsigned short)(w.y & 0xffffu), (unsigned short)(w.y >> 16)};
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                const unsigned e = 4 * c + k;
-                if (e >= first && e < end) {
-                    const float4 cf = s_cf[e4[k]];
-                    fx += cf.x;
-                    fy += cf.y;
-                    fz += cf.z;
-                }
-            }
-        }
-    }
-#else
     const unsigned short* e = inc + first;
     unsigned q = 0;
 #if NFX_FLUSH_UNROLL == 4
@@ -232,7 +206,6 @@ __device__ __forceinline__ bool node_flush(uint2 node, const unsigned short* inc
         fy += c.y;
         fz += c.z;
     }
-#endif
     if (!(fabsf(fx) <= fix_max && fabsf(fy) <= fix_max && fabsf(fz) <= fix_max)) return false;
     atomicAdd(s.facc + node.x, (unsigned long long)fix_round(fx * FORCE_FIX_SCALE));
     atomicAdd(s.facc + np + node.x, (unsigned long long)fix_round(fy * FORCE_FIX_SCALE));
