@@ -189,8 +189,8 @@ __device__ __forceinline__ bool node_flush(uint2 node, const unsigned short* inc
                                            const StateDev& s, long long np, float fix_max) {
     const unsigned first = node.y >> 16, count = node.y & 0xffffu;
     if (count == 0) return true;
-    float fx = 0.f, fy = 0.f, fz = 0.f;
     const unsigned short* e = inc + first;
+    float fx = 0.f, fy = 0.f, fz = 0.f;
     unsigned q = 0;
 #if NFX_FLUSH_UNROLL == 4
     for (; q + 4 <= count; q += 4) {
