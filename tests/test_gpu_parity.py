@@ -219,3 +219,32 @@ def test_gpu_viscoplastic_sphere_10k_steps_vs_fp64_oracle():
     assert traj < TRAJ_TOL
     assert curve < CURVE_TOL
     sim.close()
+
+
+@pytest.mark.parametrize("model,label", [(O.MODEL_SVK, "SVK"), (O.MODEL_SVKK, "SVKK"), (O.MODEL_MR, "MR")])
+def test_gpu_elastic_laws_sphere_10k_steps_vs_fp64_oracle(model, label):
+    """The other elastic laws of tetra.cl over the parity bars' horizon: Saint-Venant-Kirchhoff
+    (:94-114), its Kellnberger variant (:76-93, ten Newton steps of the polar factor) and
+    Mooney-Rivlin (:115-168, mr ratio 0.8) on the R=8 cell under a sphere of radius 2, 10^4 steps
+    against the FP64 oracle; the golden cases run these laws for a few hundred steps only."""
+    w = Workload(f"R8 {label} sphere", radius=8.0, material="mr", C10=4e-4, C01=1e-4, K=1e-2, indenter="sphere",
+                 sphere_radius=2.0, speed=1e-4, d0=None, record_every=100)
+    m = w.mesh()
+    n = 10000
+    _, E, nu, mr = w.tetra_params()
+    prob = oracle_problem(w, m)
+    prob.model = model
+    st = O.State(prob, "f64")
+    cref = st.run(n, w.record_every)
+    sim = CellSim(0)
+    w.configure(sim, m, max_rows=n // w.record_every + 2)
+    sim.set_tetra(model, E, nu, mr)
+    sim.step(n)
+    sim.record_now()
+    assert sim.status() == 0
+    assert cref[-1, 2] > 0  # the sphere pressed into the cell
+    traj, curve = rel_traj(st.positions(), sim.points()), rel_curve(cref, sim.curve())
+    print(f"R8 {label} sphere 1e4 steps: trajectory {traj:.3e} curve {curve:.3e}")
+    assert traj < TRAJ_TOL
+    assert curve < CURVE_TOL
+    sim.close()
