@@ -248,3 +248,29 @@ def test_gpu_elastic_laws_sphere_10k_steps_vs_fp64_oracle(model, label):
     assert traj < TRAJ_TOL
     assert curve < CURVE_TOL
     sim.close()
+
+
+@pytest.mark.parametrize("label", ["VV2 sphere", "integrated sphere"])
+def test_gpu_integrator_and_contact_variants_10k_steps_vs_fp64_oracle(label):
+    """The lumped-mass integrator (velocityVerlet2.cl, damping 0.05) and the integrated sphere
+    contact (InteractionSphereIntegral.cl) on the R=8 Mooney-Rivlin cell over 10^4 steps against the
+    FP64 oracle; the golden cases run them for a few hundred steps only."""
+    base = Workload(f"R8 {label}", radius=8.0, material="mr", C10=4e-4, C01=1e-4, K=1e-2, speed=1e-4,
+                    sphere_radius=2.0, record_every=100)
+    w = (base.with_(indenter="sphere", d0=None, integrator="vv2", xi=0.05) if label == "VV2 sphere"
+         else base.with_(indenter="sphere_integral", d0=0.3))
+    m = w.mesh()
+    n = 10000
+    st = O.State(oracle_problem(w, m), "f64")
+    cref = st.run(n, w.record_every)
+    sim = CellSim(0)
+    w.configure(sim, m, max_rows=n // w.record_every + 2)
+    sim.step(n)
+    sim.record_now()
+    assert sim.status() == 0
+    assert np.abs(cref[:, 2]).max() > 0
+    traj, curve = rel_traj(st.positions(), sim.points()), rel_curve(cref, sim.curve())
+    print(f"R8 {label} 1e4 steps: trajectory {traj:.3e} curve {curve:.3e}")
+    assert traj < TRAJ_TOL
+    assert curve < CURVE_TOL
+    sim.close()
