@@ -6,7 +6,8 @@ where the FP64 oracle is too slow for a long comparison.
   of a freely vibrating cell stays zero whatever the damping (VelocityVerlet.cl: v' = a v + hb
   (f + f_old) sums to a Σv + hb (Σf + Σf_old)); the fixed-point accumulation keeps each node's sum
   exact, so only per-node FP32 roundings remain.
-* Rigid motion: a translated cell is unstrained, so the element pass leaves it at rest.
+* Rigid motion: a translated cell is unstrained, so the element pass leaves it at rest; a rotated
+  one is unstrained too (objectivity), up to the FP32 rounding of its rotated edges.
 """
 
 import numpy as np
@@ -60,3 +61,26 @@ def test_translated_cell_stays_at_rest(big_mesh):
     print(f"R64 translated cell, 50 steps: max |v| {np.abs(v).max():.3e}")
     assert np.abs(v).max() < 1e-9
     s.close()
+
+
+def test_rotated_cell_is_nearly_unstressed(big_mesh):
+    """Objectivity of the finite-strain law: a cell turned rigidly by 0.3 rad is unstrained
+    (F = R, E = F F^T - I = 0), so after 20 steps its nodes move by FP32 rounding only — three
+    orders of magnitude less than those of the same cell given a 1e-2 strain instead."""
+    m = big_mesh
+    X = m.points
+    c, sn = np.cos(0.3), np.sin(0.3)
+    R = np.array([[c, -sn, 0.0], [sn, c, 0.0], [0.0, 0.0, 1.0]])
+    a = free_cell(m)
+    a.set_points(X @ R.T)
+    a.step(20)
+    b = free_cell(m)
+    b.set_points(X * np.array([1.01, 1.0, 1.0]))  # 1 % stretch along x
+    b.step(20)
+    assert a.status() == 0 and b.status() == 0
+    va, vb = np.abs(a.velocities()).max(), np.abs(b.velocities()).max()
+    print(f"R64 rotated cell, 20 steps: max |v| {va:.3e}; stretched cell {vb:.3e}")
+    assert vb > 0
+    assert va < 1e-3 * vb
+    a.close()
+    b.close()
