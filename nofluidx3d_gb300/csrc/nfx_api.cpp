@@ -168,9 +168,9 @@ int upload_cell(nfx_sim* s) {
     return NFX_OK;
 }
 
-// Element pass launch: one CTA per tile.
-cudaError_t launch_elem(nfx_sim* s, int k) {
-    return launch_tet_pass(s->mesh, s->st, table_view(s), s->cell.mat.model, k, s->stream);
+// Element pass launch: one CTA per tile (pdl: as a dependent launch, inside a run of steps).
+cudaError_t launch_elem(nfx_sim* s, int k, bool pdl = false) {
+    return launch_tet_pass(s->mesh, s->st, table_view(s), s->cell.mat.model, k, s->stream, pdl);
 }
 
 cudaError_t launch_nodes(nfx_sim* s, int k, int mode, int readout_contact, bool pdl = false) {
@@ -191,9 +191,9 @@ cudaError_t prepare_readout(nfx_sim* s, int contact) {
 
 int enqueue_steps(nfx_sim* s, int n) {
     for (int k = 0; k < n; k++) {
-        CUDA_TRY(launch_elem(s, k));
+        CUDA_TRY(launch_elem(s, k, true));                    // programmatic dependent launches
         CUDA_TRY(launch_si(s, k));
-        CUDA_TRY(launch_nodes(s, k, NODE_UPDATE, -1, true));  // programmatic dependent launch
+        CUDA_TRY(launch_nodes(s, k, NODE_UPDATE, -1, true));
     }
     CUDA_TRY(launch_advance_time(s->st, n, s->fields_every, s->record_every, s->stream));
     return NFX_OK;

@@ -423,7 +423,7 @@ int enqueue_batch_steps(nfx_batch* b, BatchDevice& D, int n) {
     for (int k = 0; k < n; k++) {
         for (BucketDev& K : D.buckets) {
             if (K.mesh.ntiles <= 0) continue;
-            BCUDA(launch_tet_pass(K.mesh, K.st, K.bd, b->model, k, b->stream));
+            BCUDA(launch_tet_pass(K.mesh, K.st, K.bd, b->model, k, b->stream, true));
             if (b->has_si) BCUDA(launch_si_pass(K.mesh, K.st, K.bd, k, false, -1, b->stream));
         }
         BCUDA(launch_node_pass(D.mesh, D.st, D.bd, D.nblocks, k, NODE_UPDATE, -1, b->stream, true));

@@ -214,9 +214,10 @@ struct NvtxRange {
 void set_error(const std::string& msg);
 
 // Kernel launchers (nfx_kernels.cu). All enqueue on `stream` and return cudaGetLastError().
-// Element pass over all tiles (one CTA per tile), material from the cell table.
+// Element pass over all tiles (one CTA per tile), material from the cell table. pdl: as a
+// programmatic dependent launch (the kernel waits before any read, so after any predecessor).
 cudaError_t launch_tet_pass(const MeshDev& m, const StateDev& s, const BatchDev& b, int model, int t_offset,
-                            cudaStream_t stream);
+                            cudaStream_t stream, bool pdl = false);
 enum NodeMode : int { NODE_UPDATE = 0, NODE_READOUT_ROW = 1, NODE_READOUT_VALUE = 2 };
 // Node pass over `nblocks` node blocks. NODE_READOUT_VALUE sums contact `readout_contact`'s force
 // per cell into force_out[cell] without updating the state.

@@ -42,6 +42,13 @@ namespace nfx {
 #ifndef NFX_TET_TRIGGER
 #define NFX_TET_TRIGGER 1
 #endif
+// The element pass as a dependent launch of the node pass before it (NFX_PDL_TET): it waits as its
+// very first instruction, before any read, so it is correct after any predecessor; what it gains
+// is only that its CTAs are resident when the node pass completes. The node pass then releases
+// its dependents as each of its CTAs starts.
+#ifndef NFX_PDL_TET
+#define NFX_PDL_TET 1
+#endif
 __device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void grid_dep_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
@@ -394,6 +401,9 @@ __global__ void __launch_bounds__(TILE, 65536 / (TILE * NFX_TET_REGS))
     // The order changes no result: tile sums enter the accumulator as integers.
 #ifndef NFX_TILE_REVERSE
 #define NFX_TILE_REVERSE 1
+#endif
+#if NFX_PDL_TET
+    grid_dep_wait();  // the node pass (or whatever preceded) has completed
 #endif
     const int b = NFX_TILE_REVERSE ? (int)(gridDim.x - 1 - blockIdx.x) : (int)blockIdx.x;
     const int j = threadIdx.x;
@@ -761,6 +771,9 @@ __global__ void __launch_bounds__(NODE_BLOCK, NFX_NODE_MIN_BLOCKS) k_node_pass(M
     __shared__ WallStep s_wall[MAX_CONTACTS];
     __shared__ float4 s_box[2];
     __shared__ int s_last;
+#if NFX_PDL_TET
+    if (threadIdx.x == 0) grid_dep_trigger();  // the next element pass may take freed SMs
+#endif
     const int cell = bd.block_cell ? __ldg(bd.block_cell + blockIdx.x) : 0;
     const CellDev& C = bd.cells[cell];
     const int i = blockIdx.x * NODE_BLOCK + threadIdx.x;
@@ -931,28 +944,41 @@ __global__ void k_vec_from_user(int np, float4* a, float2* b, int part, const lo
 // ------------------------------------------------------------------------------------------
 // Launchers
 // ------------------------------------------------------------------------------------------
+template <int MODEL, int TILE>
+static cudaError_t launch_tet(const MeshDev& m, const StateDev& s, const BatchDev& b, int t_offset, cudaStream_t st,
+                              bool pdl) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)m.ntiles);
+    cfg.blockDim = dim3(TILE);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = (NFX_PDL_TET && pdl) ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k_tet_pass<MODEL, TILE>, m, s, b, t_offset);
+}
+
 template <int TILE>
 static cudaError_t launch_tile(const MeshDev& m, const StateDev& s, const BatchDev& b, int model, int t_offset,
-                               cudaStream_t st) {
-    const dim3 grid((unsigned)m.ntiles), block(TILE);
+                               cudaStream_t st, bool pdl) {
     switch (model) {
-        case MODEL_MR: k_tet_pass<MODEL_MR, TILE><<<grid, block, 0, st>>>(m, s, b, t_offset); break;
-        case MODEL_SVK: k_tet_pass<MODEL_SVK, TILE><<<grid, block, 0, st>>>(m, s, b, t_offset); break;
-        case MODEL_SVKK: k_tet_pass<MODEL_SVKK, TILE><<<grid, block, 0, st>>>(m, s, b, t_offset); break;
-        case MODEL_VP: k_tet_pass<MODEL_VP, TILE><<<grid, block, 0, st>>>(m, s, b, t_offset); break;
+        case MODEL_MR: return launch_tet<MODEL_MR, TILE>(m, s, b, t_offset, st, pdl);
+        case MODEL_SVK: return launch_tet<MODEL_SVK, TILE>(m, s, b, t_offset, st, pdl);
+        case MODEL_SVKK: return launch_tet<MODEL_SVKK, TILE>(m, s, b, t_offset, st, pdl);
+        case MODEL_VP: return launch_tet<MODEL_VP, TILE>(m, s, b, t_offset, st, pdl);
         default: return cudaErrorInvalidValue;
     }
-    return cudaGetLastError();
 }
 
 cudaError_t launch_tet_pass(const MeshDev& m, const StateDev& s, const BatchDev& b, int model, int t_offset,
-                            cudaStream_t st) {
+                            cudaStream_t st, bool pdl) {
     if (m.ntiles <= 0) return cudaSuccess;
     switch (m.tile_tets) {
-        case 64: return launch_tile<64>(m, s, b, model, t_offset, st);
-        case 128: return launch_tile<128>(m, s, b, model, t_offset, st);
-        case 256: return launch_tile<256>(m, s, b, model, t_offset, st);
-        case 512: return launch_tile<512>(m, s, b, model, t_offset, st);
+        case 64: return launch_tile<64>(m, s, b, model, t_offset, st, pdl);
+        case 128: return launch_tile<128>(m, s, b, model, t_offset, st, pdl);
+        case 256: return launch_tile<256>(m, s, b, model, t_offset, st, pdl);
+        case 512: return launch_tile<512>(m, s, b, model, t_offset, st, pdl);
         default: return cudaErrorInvalidValue;
     }
 }
